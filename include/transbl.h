@@ -1,0 +1,186 @@
+/*
+ * transbl.h -- C ABI of the GB300-native per-RK4-stage hot path of the
+ * trans_bl incompressible boundary-layer DNS (vorticity-velocity form,
+ * compact finite differences in x/y, spanwise Fourier modes in z).
+ *
+ * The library keeps the whole domain resident in GPU memory and runs every
+ * loop nest of one RK stage as hand-written CUDA for sm_103a.  The entry
+ * points mirror the Fortran subroutines of the reference one for one, with
+ * the reference's argument order (output first), so that a Fortran host can
+ * bind them through ISO_C_BINDING.
+ *
+ * Conventions
+ *  - Fields are complex*16, Fortran column-major f(nx, ny, kfour): i fastest,
+ *    then j, then k; interleaved (re, im) doubles.  Host pointers passed to
+ *    the mirrors below are borrowed for the duration of the call.
+ *  - Indices inside the config (i0..i4) are 1-based, as in the reference.
+ *  - Every function returns an int status (TB_OK = 0 or a TB_ERR_* code);
+ *    tb_last_error() gives a one-line message for the last failure of the
+ *    calling thread.
+ *  - One host thread per context; contexts are independent.
+ *
+ * Reference interfaces (paths inside the trans_bl project):
+ *  par.for:1-132             compile-time parameters   -> tb_config
+ *  main_par.f:551-772        init_fi                   -> tb_create, tb_set_coefs, tb_init_fields
+ *  main_par.f:165-254        solver RK4 loop (form 0)  -> tb_rk_stage/tb_step
+ *  main_par.f:1264-1336      drv_fi                    -> tb_drv
+ *  main_par.f:1487-1574      drv_les                   -> tb_drv (my_form 4)
+ *  main_par.f:1762-1785      loop                      -> tb_loop
+ */
+#ifndef TRANSBL_H
+#define TRANSBL_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TB_OK            0
+#define TB_ERR_ARG       1  /* bad argument / config                              */
+#define TB_ERR_CUDA      2  /* CUDA runtime failure (message in tb_last_error)    */
+#define TB_ERR_NOCONV    3  /* Poisson V-cycle cap reached above the tolerance    */
+#define TB_ERR_NONFINITE 4  /* NaN/Inf met in a residual reduction                */
+#define TB_ERR_TIMEOUT   5  /* a bounded device wait gave up                       */
+#define TB_ERR_STATE     6  /* call order violated (e.g. no coefficients yet)      */
+#define TB_ERR_NOMEM     7  /* device allocation failed                            */
+
+/* Precision forms of the stage. */
+#define TB_FORM_PLAIN_FP64 0   /* drop-in: FP64 everywhere, lexicographic line-SOR */
+#define TB_FORM_MIXED      1   /* FP32 multigrid inside FP64 defect correction      */
+
+/* Runtime replacement of the compile-time parameters of par.for. */
+typedef struct tb_config {
+    int    nx;          /* imax = ptsx (whole domain, one GPU)        par.for:81-82 */
+    int    ny;          /* jmax                                        par.for:73   */
+    int    kfour;       /* stored Fourier modes K (k = 0..K-1)         par.for:106  */
+    int    kphys;       /* physical z points P, power of two, >= 4     par.for:106  */
+    int    msh;         /* multigrid levels                            par.for:102  */
+    int    my_form;     /* 0: drv_fi (+optional IBM), 4: drv_les       par.for:14   */
+    int    i0, i1, i2, i3, i4;  /* buffer ramp end, TS strip, damping  par.for:21,88 */
+    int    stpp;        /* time steps per forcing period               par.for:92   */
+    int    max_vcycles; /* V-cycle cap (11 in the reference)  poisson_par.f:33      */
+    int    ibm;         /* 1: add immersed-boundary force (cvirt)                   */
+    int    precision;   /* TB_FORM_PLAIN_FP64 or TB_FORM_MIXED                      */
+    int    les_damping; /* 0: reference cubic damping, 1: van Driest [1-e^{-y+/A}]^2*/
+    double Re;          /* U L / nu                                    par.for:41   */
+    double dx;          /* uniform x spacing                           par.for:83   */
+    double dy;          /* first wall-normal spacing dy0               par.for:73   */
+    double stf;         /* geometric stretching factor in y            par.for:75   */
+    double x0;          /* x of i = 1                                  par.for:41   */
+    double alpha;       /* streamwise wavenumber (top Poisson BC)      par.for:56   */
+    double omega;       /* forcing frequency; dt = 2 pi / omega / stpp par.for:57,93*/
+    double beta;        /* spanwise wavenumber                         par.for:70   */
+    double fac_y;       /* y scaling (1 or Re)                         par.for:45   */
+    double alphaf;      /* compact filter alpha_f (0.48)               par.for:116  */
+    double tol_stage;   /* Poisson max-defect tolerance, stages 1-3 (1e-5) main_par.f:187 */
+    double tol_final;   /* Poisson max-defect tolerance, stage 4 (1e-6)   main_par.f:247 */
+    double C_s;         /* Smagorinsky constant                        par.for:126  */
+    double A_plus;      /* damping length in wall units (25)           les_par.f:195 */
+    double irf;         /* IBM feedback gain (-0.1 Re)                 par.for:123  */
+    double ibm_xc, ibm_zc, ibm_h, ibm_R;  /* roughness centre, height, radius  immersed_par.f:111-120 */
+    /* Wall suction/blowing forcing per Fourier mode (ts2d_pert/ts3d_pert,
+       main_par.f:1613-1685): uy(i,1,k) = A_k fcx(i) sin(omega (t+tau) dt + phi_k). */
+    int    n_forced;            /* number of forced modes (<= 4)                    */
+    int    forced_mode[4];      /* 0-based Fourier mode index                       */
+    double forced_amp[4];       /* amplitude A_k                                    */
+    double forced_phase[4];     /* phase phi_k (0 in the reference)                 */
+} tb_config;
+
+typedef struct tb_ctx tb_ctx;
+
+/* Per-solve Poisson statistics (poisson_par.f:58-60 prints k, vcycles-1, err). */
+typedef struct tb_poisson_stats {
+    int    vcycles[256];   /* V-cycles taken per mode in the last poi_uy     */
+    double residual[256];  /* last max|defect| per mode                      */
+    int    total_vcycles;  /* accumulated over the context's lifetime        */
+    int    solves;         /* number of poi_uy calls accumulated             */
+    int    noconv;         /* modes that hit the cap in the last poi_uy      */
+} tb_poisson_stats;
+
+const char* tb_last_error(void);
+
+/* Fill cfg with the reference defaults of par.for scaled to a tiny grid. */
+int tb_config_default(tb_config* cfg);
+/* Derived quantities (dt = 2 pi / omega / stpp, par.for:93). */
+double tb_dt(const tb_config* cfg);
+
+/* ---- host set-up (pre_processing/) ---------------------------------- */
+/* Number of doubles in a coefficient blob for msh levels: 100 + 24 msh.
+   Layout = records 1..16 of pre_processing/coefs.bin (coef_generation.f90:38-53),
+   record 1 being fp_fd_coef_e(6). */
+int tb_coef_count(int msh);
+/* Stretched-grid compact / Poisson / wall coefficients
+   (pre_processing/derivative.f90:1762-1882, at_wall.f90:1499). */
+int tb_generate_coefs(double stf, int msh, double* blob);
+/* Compact first-point first-derivative weights fp_fd_coef(7)
+   (derivative.f90:15-108); record 1 of pre_processing/coefs.bin holds these. */
+int tb_generate_fp_fd(double stf, double* out7);
+/* Falkner-Skan / Blasius wall shear by Newton shooting (fs_sch.f90:11-54):
+   returns f''(0) for pressure-gradient parameter beta_fs. */
+int tb_fs_wall_shear(double beta_fs, double* fpp);
+/* Base flow on the (nx, ny) grid (fs_sch.f90:58-162), column-major reals. */
+int tb_baseflow_fs(const tb_config* cfg, double beta_fs, double* uxb, double* uyb, double* wzb);
+
+/* ---- lifecycle --------------------------------------------------------- */
+int tb_create(const tb_config* cfg, tb_ctx** out);
+int tb_destroy(tb_ctx* ctx);
+int tb_set_coefs(tb_ctx* ctx, const double* blob);
+int tb_set_baseflow(tb_ctx* ctx, const double* uxb, const double* uyb, const double* wzb);
+/* init_fi (main_par.f:551-772): zero every field, base flow into mode 0,
+   buffer ramps, filter and x-penta factors, forcing shape, IBM delta. */
+int tb_init_fields(tb_ctx* ctx);
+int tb_put_state(tb_ctx* ctx, const double* ux, const double* uy, const double* uz,
+                 const double* wx, const double* wy, const double* wz);
+int tb_get_state(tb_ctx* ctx, double* ux, double* uy, double* uz,
+                 double* wx, double* wy, double* wz);
+/* d2uydx2(nx, K) wall forcing curvature (common /derw/). */
+int tb_put_wall(tb_ctx* ctx, const double* d2uydx2);
+int tb_get_wall(tb_ctx* ctx, double* d2uydx2);
+int tb_synchronize(tb_ctx* ctx);
+
+/* ---- time stepping (main_par.f:165-254) -------------------------------- */
+int tb_rk_stage(tb_ctx* ctx, int stage, int t);   /* stage 1..4 of step t        */
+int tb_step(tb_ctx* ctx, int t);                  /* four stages                 */
+int tb_steps(tb_ctx* ctx, int t0, int nsteps);    /* t0 .. t0+nsteps-1           */
+int tb_get_poisson_stats(tb_ctx* ctx, tb_poisson_stats* st);
+
+/* ---- per-subroutine mirrors (host pointers, copy in / out) ------------ */
+int tb_derparx (tb_ctx* ctx, double* ddx,   const double* fc);  /* derivs_par.f:80  */
+int tb_derparxx(tb_ctx* ctx, double* d2dx2, const double* fc);  /* derivs_par.f:98  */
+int tb_dery    (tb_ctx* ctx, double* ddy,   const double* fc);  /* derivs_par.f:116 */
+int tb_deryfv  (tb_ctx* ctx, double* ddy,   const double* fc);  /* derivs_par.f:148 */
+int tb_deryy   (tb_ctx* ctx, double* d2dy2, const double* fc);  /* derivs_par.f:164 */
+/* nlterms_fi on the context state (nlterms_par.f:41): a, b, c out. */
+int tb_nlterms (tb_ctx* ctx, double* a, double* b, double* c);
+/* drv_fi / drv_les on the context state: dvx, dvy, dvz out (main_par.f:1264,1487). */
+int tb_drv     (tb_ctx* ctx, double* dvx, double* dvy, double* dvz);
+/* loop(erro) on the context state (main_par.f:1762). */
+int tb_loop    (tb_ctx* ctx, double erro);
+int tb_filter_trid(tb_ctx* ctx);                                 /* filter_par.f:144 */
+int tb_bzone   (tb_ctx* ctx);                                    /* loop_par.f:6     */
+int tb_bzonew  (tb_ctx* ctx);                                    /* loop_par.f:691   */
+int tb_outuy   (tb_ctx* ctx, double* dwzdx);                     /* loop_par.f:48    */
+int tb_poi_uy  (tb_ctx* ctx, const double* dwzdx, double erro);  /* poisson_par.f:6  */
+int tb_poi_ux  (tb_ctx* ctx, double* duydy);                     /* loop_par.f:428   */
+int tb_poi_uz  (tb_ctx* ctx, const double* duydy);               /* loop_par.f:569   */
+int tb_wx_wall (tb_ctx* ctx, double* lapv);                      /* loop_par.f:174   */
+int tb_wz_wall (tb_ctx* ctx, const double* lapv);                /* loop_par.f:361   */
+int tb_ts_pert (tb_ctx* ctx, int t, double tempt);               /* main_par.f:1613  */
+int tb_les_terms(tb_ctx* ctx, double* fx, double* fy, double* fz); /* les_par.f:6    */
+int tb_cvirt   (tb_ctx* ctx, double* fx, double* fy, double* fz);  /* immersed_par.f:262 */
+/* Spanwise transforms of one field (nlterms_par.f:303,364).
+   phys: real (nx, ny, kphys); four: complex (nx, ny, kfour). */
+int tb_f_to_p  (tb_ctx* ctx, double* phys, const double* four);
+int tb_p_to_f  (tb_ctx* ctx, double* four, const double* phys);
+
+/* ---- device-resident access (no host copies) ------------------------- */
+/* Device pointers of the resident fields: which = 0..5 for ux,uy,uz,wx,wy,wz. */
+int tb_device_field(tb_ctx* ctx, int which, void** dptr);
+/* CUDA stream (cudaStream_t) every kernel of this context is launched on. */
+int tb_stream(tb_ctx* ctx, void** stream);
+/* Kernel launches issued by this context so far (for launch accounting). */
+long long tb_launch_count(tb_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TRANSBL_H */

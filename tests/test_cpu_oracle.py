@@ -1,0 +1,77 @@
+"""Properties of the CPU oracle (the checker of the GPU library)."""
+import numpy as np
+import pytest
+
+from tests.helpers import perturbed_state, rel, small_case
+
+
+@pytest.fixture(scope="module")
+def case(lib_built, oracle_built):
+    cfg, coefs, base = small_case()
+    return cfg, coefs, base, oracle_built
+
+
+def test_x_derivatives_exact_on_polynomials(case):
+    cfg, coefs, base, ora = case
+    o = ora.Oracle(cfg, coefs, base)
+    x = cfg.x0 + cfg.dx * np.arange(cfg.nx)
+    f = np.zeros(o.shape, complex)
+    f[:] = (x ** 4 - 2 * x ** 3 + x)[None, None, :]
+    d1 = o.derparx(f)
+    d2 = o.derparxx(f)
+    assert rel(d1[0, 3], 4 * x ** 3 - 6 * x ** 2 + 1) < 1e-9
+    assert rel(d2[0, 3], 12 * x ** 2 - 12 * x) < 1e-8
+
+
+def test_y_derivatives_exact_on_polynomials(case):
+    cfg, coefs, base, ora = case
+    o = ora.Oracle(cfg, coefs, base)
+    j = np.arange(cfg.ny)
+    y = cfg.dy * (cfg.stf ** j - 1) / (cfg.stf - 1)
+    f = np.zeros(o.shape, complex)
+    f[:] = (y ** 3 - y ** 2)[None, :, None]
+    d1 = o.dery(f)
+    d2 = o.deryy(f)
+    assert rel(d1[0, :, 5], 3 * y ** 2 - 2 * y) < 1e-8
+    assert rel(d2[0, :, 5], 6 * y - 2) < 1e-8
+
+
+def test_spanwise_transform_convention_and_roundtrip(case):
+    cfg, coefs, base, ora = case
+    o = ora.Oracle(cfg, coefs, base)
+    rng = np.random.default_rng(1)
+    c = rng.normal(size=o.shape) + 1j * rng.normal(size=o.shape)
+    c[0] = c[0].real
+    p = o.f_to_p(c)
+    P, K = cfg.kphys, cfg.kfour
+    n = np.arange(P)
+    ref = np.zeros((P,) + c.shape[1:])
+    for k in range(K):
+        w = np.exp(-2j * np.pi * k * n / P)[:, None, None]
+        ref += (c[k][None] * w).real
+    assert rel(p, ref) < 1e-13
+    back = o.p_to_f(p)
+    assert rel(back, c) < 1e-12
+
+
+def test_poisson_reaches_tolerance(case):
+    cfg, coefs, base, ora = case
+    o = ora.Oracle(cfg, coefs, base)
+    rng = np.random.default_rng(2)
+    o.put_state(perturbed_state(cfg, base, rng))
+    dwzdx = o.outuy()
+    o.poi_uy(dwzdx, 1e-3)
+    v, r = o.poisson_stats()
+    assert all(x < cfg.max_vcycles for x in v), v
+    assert np.all(r < 1e-3)
+
+
+def test_stage_runs_finite(case):
+    cfg, coefs, base, ora = case
+    o = ora.Oracle(cfg, coefs, base)
+    for t in (1, 2):
+        o.step(t)
+    s = o.get_state()
+    for n, f in s.items():
+        assert np.all(np.isfinite(f)), n
+    assert np.max(np.abs(s["uy"][0, 0])) > 0  # the wall forcing is on

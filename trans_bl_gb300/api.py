@@ -1,0 +1,312 @@
+"""ctypes binding of the C ABI in include/transbl.h.
+
+Fields are numpy complex128 arrays of shape (kfour, ny, nx), C-contiguous:
+the same memory as the reference's Fortran complex*16 f(nx, ny, kfour).
+The library is the CUDA build in this package directory; there is no CPU
+fallback -- loading fails loudly when it is missing.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libtransbl.so")
+
+TB_OK = 0
+TB_ERR = {1: "TB_ERR_ARG", 2: "TB_ERR_CUDA", 3: "TB_ERR_NOCONV", 4: "TB_ERR_NONFINITE",
+          5: "TB_ERR_TIMEOUT", 6: "TB_ERR_STATE", 7: "TB_ERR_NOMEM"}
+FORM_PLAIN_FP64 = 0
+FORM_MIXED = 1
+
+
+class TbConfig(C.Structure):
+    """Mirror of struct tb_config (runtime replacement of par.for)."""
+    _fields_ = [(n, C.c_int) for n in (
+        "nx", "ny", "kfour", "kphys", "msh", "my_form", "i0", "i1", "i2", "i3", "i4", "stpp",
+        "max_vcycles", "ibm", "precision", "les_damping")] + \
+        [(n, C.c_double) for n in (
+            "Re", "dx", "dy", "stf", "x0", "alpha", "omega", "beta", "fac_y", "alphaf", "tol_stage",
+            "tol_final", "C_s", "A_plus", "irf", "ibm_xc", "ibm_zc", "ibm_h", "ibm_R")] + \
+        [("n_forced", C.c_int), ("forced_mode", C.c_int * 4), ("forced_amp", C.c_double * 4),
+         ("forced_phase", C.c_double * 4)]
+
+    def as_dict(self):
+        d = {}
+        for n, _ in self._fields_:
+            v = getattr(self, n)
+            d[n] = list(v) if hasattr(v, "__len__") else v
+        return d
+
+
+class PoissonStats(C.Structure):
+    _fields_ = [("vcycles", C.c_int * 256), ("residual", C.c_double * 256), ("total_vcycles", C.c_int),
+                ("solves", C.c_int), ("noconv", C.c_int)]
+
+
+class TbError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise TbError("CUDA library %s is missing: build it with `python -m trans_bl_gb300.build`" % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    D = C.POINTER(C.c_double)
+    lib.tb_last_error.restype = C.c_char_p
+    lib.tb_dt.restype = C.c_double
+    lib.tb_dt.argtypes = [C.POINTER(TbConfig)]
+    lib.tb_launch_count.restype = C.c_longlong
+    lib.tb_launch_count.argtypes = [P]
+    lib.tb_create.argtypes = [C.POINTER(TbConfig), C.POINTER(P)]
+    lib.tb_config_default.argtypes = [C.POINTER(TbConfig)]
+    lib.tb_coef_count.argtypes = [C.c_int]
+    lib.tb_generate_coefs.argtypes = [C.c_double, C.c_int, D]
+    lib.tb_generate_fp_fd.argtypes = [C.c_double, D]
+    lib.tb_fs_wall_shear.argtypes = [C.c_double, D]
+    lib.tb_baseflow_fs.argtypes = [C.POINTER(TbConfig), C.c_double, D, D, D]
+    for n in ("tb_destroy", "tb_init_fields", "tb_synchronize", "tb_filter_trid", "tb_bzone", "tb_bzonew"):
+        getattr(lib, n).argtypes = [P]
+    lib.tb_set_coefs.argtypes = [P, D]
+    lib.tb_set_baseflow.argtypes = [P, D, D, D]
+    lib.tb_put_state.argtypes = [P] + [D] * 6
+    lib.tb_get_state.argtypes = [P] + [D] * 6
+    lib.tb_put_wall.argtypes = [P, D]
+    lib.tb_get_wall.argtypes = [P, D]
+    lib.tb_rk_stage.argtypes = [P, C.c_int, C.c_int]
+    lib.tb_step.argtypes = [P, C.c_int]
+    lib.tb_steps.argtypes = [P, C.c_int, C.c_int]
+    lib.tb_get_poisson_stats.argtypes = [P, C.POINTER(PoissonStats)]
+    for n in ("tb_derparx", "tb_derparxx", "tb_dery", "tb_deryfv", "tb_deryy", "tb_f_to_p", "tb_p_to_f"):
+        getattr(lib, n).argtypes = [P, D, D]
+    for n in ("tb_nlterms", "tb_drv", "tb_les_terms", "tb_cvirt"):
+        getattr(lib, n).argtypes = [P, D, D, D]
+    lib.tb_loop.argtypes = [P, C.c_double]
+    lib.tb_outuy.argtypes = [P, D]
+    lib.tb_poi_uy.argtypes = [P, D, C.c_double]
+    lib.tb_poi_ux.argtypes = [P, D]
+    lib.tb_poi_uz.argtypes = [P, D]
+    lib.tb_wx_wall.argtypes = [P, D]
+    lib.tb_wz_wall.argtypes = [P, D]
+    lib.tb_ts_pert.argtypes = [P, C.c_int, C.c_double]
+    lib.tb_device_field.argtypes = [P, C.c_int, C.POINTER(P)]
+    lib.tb_stream.argtypes = [P, C.POINTER(P)]
+    _lib = lib
+    return lib
+
+
+def check(rc, what=""):
+    if rc != TB_OK:
+        msg = load().tb_last_error().decode(errors="replace")
+        raise TbError("%s failed: %s (%s)" % (what, TB_ERR.get(rc, rc), msg))
+
+
+def dptr(a):
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def default_config(**kw):
+    cfg = TbConfig()
+    check(load().tb_config_default(C.byref(cfg)), "tb_config_default")
+    for k, v in kw.items():
+        if k in ("forced_mode", "forced_amp", "forced_phase"):
+            arr = getattr(cfg, k)
+            for q in range(4):
+                arr[q] = v[q] if q < len(v) else 0
+        else:
+            setattr(cfg, k, v)
+    return cfg
+
+
+def coef_count(msh):
+    return load().tb_coef_count(msh)
+
+
+def generate_coefs(stf, msh):
+    blob = np.zeros(coef_count(msh))
+    check(load().tb_generate_coefs(float(stf), int(msh), dptr(blob)), "tb_generate_coefs")
+    return blob
+
+
+def generate_fp_fd(stf):
+    out = np.zeros(7)
+    check(load().tb_generate_fp_fd(float(stf), dptr(out)), "tb_generate_fp_fd")
+    return out
+
+
+def fs_wall_shear(beta_fs=0.0):
+    v = np.zeros(1)
+    check(load().tb_fs_wall_shear(float(beta_fs), dptr(v)), "tb_fs_wall_shear")
+    return float(v[0])
+
+
+def baseflow_fs(cfg, beta_fs=0.0):
+    shape = (cfg.ny, cfg.nx)
+    ux, uy, wz = np.zeros(shape), np.zeros(shape), np.zeros(shape)
+    check(load().tb_baseflow_fs(C.byref(cfg), float(beta_fs), dptr(ux), dptr(uy), dptr(wz)), "tb_baseflow_fs")
+    return ux, uy, wz
+
+
+class Context:
+    """One simulation resident on the current CUDA device (tb_ctx)."""
+
+    def __init__(self, cfg, coefs=None, baseflow=None, init=True):
+        self.lib = load()
+        self.cfg = cfg
+        h = C.c_void_p()
+        check(self.lib.tb_create(C.byref(cfg), C.byref(h)), "tb_create")
+        self.h = h
+        self.shape = (cfg.kfour, cfg.ny, cfg.nx)
+        if coefs is not None:
+            self.set_coefs(coefs)
+        if baseflow is not None:
+            self.set_baseflow(*baseflow)
+            if init and coefs is not None:
+                self.init_fields()
+
+    def close(self):
+        if self.h:
+            self.lib.tb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, rc, what):
+        check(rc, what)
+
+    def field(self):
+        return np.zeros(self.shape, dtype=np.complex128)
+
+    def set_coefs(self, blob):
+        blob = np.ascontiguousarray(blob, dtype=np.float64)
+        self._c(self.lib.tb_set_coefs(self.h, dptr(blob)), "tb_set_coefs")
+
+    def set_baseflow(self, uxb, uyb, wzb):
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (uxb, uyb, wzb)]
+        self._c(self.lib.tb_set_baseflow(self.h, *[dptr(x) for x in a]), "tb_set_baseflow")
+
+    def init_fields(self):
+        self._c(self.lib.tb_init_fields(self.h), "tb_init_fields")
+
+    def put_state(self, state):
+        a = [np.ascontiguousarray(state[n], dtype=np.complex128) for n in ("ux", "uy", "uz", "wx", "wy", "wz")]
+        self._c(self.lib.tb_put_state(self.h, *[dptr(x.view(np.float64)) for x in a]), "tb_put_state")
+
+    def get_state(self):
+        out = {n: self.field() for n in ("ux", "uy", "uz", "wx", "wy", "wz")}
+        self._c(self.lib.tb_get_state(self.h, *[dptr(out[n].view(np.float64)) for n in
+                                                ("ux", "uy", "uz", "wx", "wy", "wz")]), "tb_get_state")
+        return out
+
+    def put_wall(self, d2uydx2):
+        a = np.ascontiguousarray(d2uydx2, dtype=np.complex128)
+        self._c(self.lib.tb_put_wall(self.h, dptr(a.view(np.float64))), "tb_put_wall")
+
+    def get_wall(self):
+        a = np.zeros((self.cfg.kfour, self.cfg.nx), dtype=np.complex128)
+        self._c(self.lib.tb_get_wall(self.h, dptr(a.view(np.float64))), "tb_get_wall")
+        return a
+
+    def rk_stage(self, stage, t):
+        self._c(self.lib.tb_rk_stage(self.h, stage, t), "tb_rk_stage")
+
+    def step(self, t):
+        self._c(self.lib.tb_step(self.h, t), "tb_step")
+
+    def steps(self, t0, n):
+        self._c(self.lib.tb_steps(self.h, t0, n), "tb_steps")
+
+    def synchronize(self):
+        self._c(self.lib.tb_synchronize(self.h), "tb_synchronize")
+
+    def poisson_stats(self):
+        st = PoissonStats()
+        self._c(self.lib.tb_get_poisson_stats(self.h, C.byref(st)), "tb_get_poisson_stats")
+        K = self.cfg.kfour
+        return {"vcycles": list(st.vcycles[:K]), "residual": list(st.residual[:K]),
+                "total_vcycles": st.total_vcycles, "solves": st.solves, "noconv": st.noconv}
+
+    def launch_count(self):
+        return int(self.lib.tb_launch_count(self.h))
+
+    # per-subroutine mirrors -------------------------------------------------
+    def _unary(self, name, f):
+        f = np.ascontiguousarray(f, dtype=np.complex128)
+        out = self.field()
+        self._c(getattr(self.lib, name)(self.h, dptr(out.view(np.float64)), dptr(f.view(np.float64))), name)
+        return out
+
+    def derparx(self, f): return self._unary("tb_derparx", f)
+    def derparxx(self, f): return self._unary("tb_derparxx", f)
+    def dery(self, f): return self._unary("tb_dery", f)
+    def deryfv(self, f): return self._unary("tb_deryfv", f)
+    def deryy(self, f): return self._unary("tb_deryy", f)
+
+    def _three(self, name):
+        a, b, c = self.field(), self.field(), self.field()
+        self._c(getattr(self.lib, name)(self.h, *[dptr(x.view(np.float64)) for x in (a, b, c)]), name)
+        return a, b, c
+
+    def nlterms(self): return self._three("tb_nlterms")
+    def drv(self): return self._three("tb_drv")
+    def les_terms(self): return self._three("tb_les_terms")
+    def cvirt(self): return self._three("tb_cvirt")
+
+    def loop(self, erro): self._c(self.lib.tb_loop(self.h, float(erro)), "tb_loop")
+    def filter_trid(self): self._c(self.lib.tb_filter_trid(self.h), "tb_filter_trid")
+    def bzone(self): self._c(self.lib.tb_bzone(self.h), "tb_bzone")
+    def bzonew(self): self._c(self.lib.tb_bzonew(self.h), "tb_bzonew")
+
+    def outuy(self):
+        out = self.field()
+        self._c(self.lib.tb_outuy(self.h, dptr(out.view(np.float64))), "tb_outuy")
+        return out
+
+    def poi_uy(self, dwzdx, erro):
+        a = np.ascontiguousarray(dwzdx, dtype=np.complex128)
+        self._c(self.lib.tb_poi_uy(self.h, dptr(a.view(np.float64)), float(erro)), "tb_poi_uy")
+
+    def poi_ux(self):
+        out = self.field()
+        self._c(self.lib.tb_poi_ux(self.h, dptr(out.view(np.float64))), "tb_poi_ux")
+        return out
+
+    def poi_uz(self, duydy):
+        a = np.ascontiguousarray(duydy, dtype=np.complex128)
+        self._c(self.lib.tb_poi_uz(self.h, dptr(a.view(np.float64))), "tb_poi_uz")
+
+    def wx_wall(self):
+        out = np.zeros((self.cfg.kfour, self.cfg.nx), dtype=np.complex128)
+        self._c(self.lib.tb_wx_wall(self.h, dptr(out.view(np.float64))), "tb_wx_wall")
+        return out
+
+    def wz_wall(self, lapv):
+        a = np.ascontiguousarray(lapv, dtype=np.complex128)
+        self._c(self.lib.tb_wz_wall(self.h, dptr(a.view(np.float64))), "tb_wz_wall")
+
+    def ts_pert(self, t, tempt):
+        self._c(self.lib.tb_ts_pert(self.h, int(t), float(tempt)), "tb_ts_pert")
+
+    def f_to_p(self, four):
+        four = np.ascontiguousarray(four, dtype=np.complex128)
+        out = np.zeros((self.cfg.kphys, self.cfg.ny, self.cfg.nx))
+        self._c(self.lib.tb_f_to_p(self.h, dptr(out), dptr(four.view(np.float64))), "tb_f_to_p")
+        return out
+
+    def p_to_f(self, phys):
+        phys = np.ascontiguousarray(phys, dtype=np.float64)
+        out = self.field()
+        self._c(self.lib.tb_p_to_f(self.h, dptr(out.view(np.float64)), dptr(phys)), "tb_p_to_f")
+        return out

@@ -1,0 +1,78 @@
+"""Workload definitions: synthetic Blasius/TS set-ups of the benchmark sizes.
+
+No dataset is involved: every input is generated -- the Blasius base flow by
+the Falkner-Skan shooting of the library (pre_processing/fs_sch.f90), the
+compact-scheme tables by the library's coefficient generator
+(pre_processing/derivative.f90), and the wall forcing (ts2d_pert/ts3d_pert,
+main_par.f:1613-1685) with phases drawn from a seeded generator.
+
+Non-dimensionalisation follows the reference with fac_y = 1: lengths in units
+of L = x0 (the inflow station), Re = U L / nu, time in L / U.  At the inflow
+Re_delta* = 1.7208 sqrt(Re) (Blasius).
+"""
+import math
+
+import numpy as np
+
+from . import api
+
+BLASIUS_DSTAR = 1.7208  # delta* sqrt(U/(nu x)) of the Blasius profile
+
+
+def blasius_ts_config(nx, ny, kfour, kphys, msh, stf=1.02, re_dstar=1000.0, F=1e-4, n_lambda=12.0,
+                      y_top_dstar=40.0, steps_per_period=256, beta_dstar=0.2, amp2d=1e-5, amp3d=0.0,
+                      seed=20261203, tol=1e-10, max_vcycles=11, precision=api.FORM_PLAIN_FP64, my_form=0,
+                      strip=(3.0, 4.0)):
+    """tb_config of a flat-plate TS forcing case on an (nx, ny, kfour) grid."""
+    Re = (re_dstar / BLASIUS_DSTAR) ** 2
+    dstar = BLASIUS_DSTAR / math.sqrt(Re)          # at x0 = 1
+    omega = F * Re                                 # F = omega nu / U^2
+    alpha = 0.26 / dstar                           # TS wavenumber estimate (alpha_r delta* ~ 0.26)
+    lam = 2.0 * math.pi / alpha
+    dx = n_lambda * lam / (nx - 1)
+    y_top = y_top_dstar * dstar
+    dy0 = y_top * (stf - 1.0) / (stf ** (ny - 1) - 1.0) if stf != 1.0 else y_top / (ny - 1)
+    i1 = int(round(1 + strip[0] * lam / dx))
+    i2 = int(round(1 + strip[1] * lam / dx))
+    i0 = max(5, int(round(0.025 * nx)))
+    i3 = int(round(0.80 * nx))
+    i4 = int(round(0.90 * nx))
+    rng = np.random.default_rng(seed)
+    modes, amps, phases = [0], [amp2d], [float(rng.uniform(0, 2 * math.pi))]
+    if amp3d > 0 and kfour > 1:
+        modes.append(1); amps.append(amp3d); phases.append(float(rng.uniform(0, 2 * math.pi)))
+    cfg = api.default_config(
+        nx=nx, ny=ny, kfour=kfour, kphys=kphys, msh=msh, my_form=my_form, i0=i0, i1=i1, i2=i2, i3=i3, i4=i4,
+        stpp=steps_per_period, max_vcycles=max_vcycles, precision=precision,
+        Re=Re, dx=dx, dy=dy0, stf=stf, x0=1.0, alpha=alpha, omega=omega, beta=beta_dstar / dstar, fac_y=1.0,
+        alphaf=0.48, tol_stage=tol, tol_final=tol, irf=-0.1 * Re, n_forced=len(modes),
+        forced_mode=modes, forced_amp=amps, forced_phase=phases)
+    return cfg
+
+
+# Benchmark workloads (grid sizes of the reference's headline configurations).
+def config1(**kw):
+    """2D: nx=385, ny=129, one Fourier mode (P=2), 3-level multigrid."""
+    return blasius_ts_config(385, 129, 1, 2, 3, **kw)
+
+
+def config2(**kw):
+    """3D: nx=1025, ny=193, 32 modes (P=64), 2D TS + oblique pair, 4-level multigrid."""
+    kw.setdefault("amp2d", 1e-4)
+    kw.setdefault("amp3d", 1e-5)
+    return blasius_ts_config(1025, 193, 32, 64, 4, **kw)
+
+
+def small(nx=65, ny=33, kfour=4, kphys=8, msh=3, **kw):
+    """A small grid for parity tests (seconds on the CPU oracle)."""
+    kw.setdefault("amp3d", 1e-5)
+    kw.setdefault("n_lambda", 4.0)
+    kw.setdefault("strip", (1.0, 1.6))
+    return blasius_ts_config(nx, ny, kfour, kphys, msh, **kw)
+
+
+def setup_inputs(cfg):
+    """Coefficient blob and Blasius base flow for cfg."""
+    coefs = api.generate_coefs(cfg.stf, cfg.msh)
+    base = api.baseflow_fs(cfg, 0.0)
+    return coefs, base

@@ -1,0 +1,158 @@
+// tb_internal.h -- shared definitions of the GB300 trans_bl stage library.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "../../include/transbl.h"
+
+#define TB_MAX_MSH 6
+#define TB_MAX_K 256
+
+typedef double2 cplx;  // complex*16 as (re, im)
+
+// Error plumbing ------------------------------------------------------------
+void tb_set_error(const char* fmt, ...);
+#define TB_CUDA(call)                                                                      \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            tb_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+            return TB_ERR_CUDA;                                                            \
+        }                                                                                  \
+    } while (0)
+#define TB_CHECK_LAUNCH(ctx)                                                               \
+    do {                                                                                   \
+        cudaError_t e_ = cudaGetLastError();                                               \
+        if (e_ != cudaSuccess) {                                                           \
+            tb_set_error("%s:%d kernel launch: %s", __FILE__, __LINE__, cudaGetErrorString(e_)); \
+            return TB_ERR_CUDA;                                                            \
+        }                                                                                  \
+        (ctx)->launches++;                                                                 \
+    } while (0)
+
+// Device-side line operator tables ----------------------------------------
+// Thomas factors of a constant tridiagonal LHS: forward u_i = (r_i - a_i u_{i-1}) * ib_i,
+// backward u_i -= g_{i+1} u_{i+1}  (tridparx/tridy, derivs_par.f:775-975).
+struct TriLHS {
+    double* a;   // (n)
+    double* g;   // (n) gam
+    double* ib;  // (n) 1/bet
+};
+// Row weights of the stretched-y compact RHS: row j (0-based) is
+// sum_m w[7*j+m] * f[j + off[j] + m], m < cnt[j].
+struct YRhs {
+    double* w;   // (ny*7)
+    int* off;    // (ny)
+    int* cnt;    // (ny)
+};
+// Pentadiagonal x-LU of lhs5 per Fourier mode (penta_par.f:6-50): lu(i,c) with
+// reciprocal diagonal; one block of 5*nx per mode.
+struct PentaX {
+    double* lu;   // (K, 5, nx): [k][c][i], c = 0..4 -> lu(:,1..5), c = 2 holds 1/lu(:,3)
+};
+// Banded y-LU of the Poisson line operator (band5_poi) per mode, level and
+// column type (0 centre, 1 border): L1_j, L2_j, U1_j, U2_j, 1/D_j (0-based rows).
+struct PoiBand {
+    double* t;   // [type][level][k][5][ny]
+};
+
+struct TbGrid {
+    int nx, ny, K, P, msh;
+    int ptsx[TB_MAX_MSH], ptsy[TB_MAX_MSH];
+    size_t lvl_off[TB_MAX_MSH];  // element offsets of each level inside a per-mode work block
+    size_t lvl_elems;             // per-mode work block (sum of ptsx*ptsy over levels)
+};
+
+struct tb_ctx {
+    tb_config cfg;
+    TbGrid g;
+    double dt, dt2, dt6, dz;
+    cudaStream_t stream = nullptr;
+    long long launches = 0;
+    bool have_coefs = false, have_base = false, inited = false;
+    int device = 0;
+
+    // host copies of coefficient tables
+    std::vector<double> coefs;            // blob
+    std::vector<double> h_qdy, h_qdy2;    // v_qdy(ny), v_qdy2(ny*msh)
+    std::vector<double> h_dx2;            // v_dx2(msh)
+    std::vector<double> h_k2b2;           // v_k2b2(K)
+    std::vector<double> h_bdfc, h_fcx, h_fcllx, h_gibbs, h_uxb, h_uyb, h_wzb, h_duexmdx;
+
+    // device state (comm.var) and RK storage
+    cplx *ux = nullptr, *uy = nullptr, *uz = nullptr, *wx = nullptr, *wy = nullptr, *wz = nullptr;
+    cplx *wx1 = nullptr, *wy1 = nullptr, *wz1 = nullptr;
+    cplx *dv1x = nullptr, *dv1y = nullptr, *dv1z = nullptr, *dv2x = nullptr, *dv2y = nullptr, *dv2z = nullptr;
+    cplx* d2uydx2 = nullptr;     // (nx, K)
+    cplx* lapv = nullptr;        // (nx, K)
+    cplx* tmp[24] = {nullptr};   // work fields (nx, ny, K)
+    double* uxb = nullptr; double* uyb = nullptr; double* wzb = nullptr; double* duexmdx = nullptr;
+    double* bdfc = nullptr; double* fcx = nullptr; double* fcllx = nullptr; double* gibbs = nullptr;
+    double* delta_no = nullptr;  // (nx, ny, P) IBM indicator
+    double* k2b2 = nullptr;      // (K)
+    // line-operator tables
+    TriLHS tx1, tx2, tfil, ty1, tyfv, ty2;
+    YRhs ry1, ryfv, ry2;
+    PentaX px;
+    PoiBand pb;
+    // Poisson work (per mode blocks of lvl_elems complex): fc, sc, fct
+    cplx *pfc = nullptr, *psc = nullptr, *pfct = nullptr, *pdef = nullptr;
+    double* pcarry = nullptr;    // precomputed chunk propagators of the line solve
+    int* pstate = nullptr;       // per mode: [0] active, [1] vcycles done
+    double* perr = nullptr;      // per mode max|defect|
+    double* pqdy2 = nullptr;     // v_qdy2 on device (ny*msh)
+    double* pcoef = nullptr;     // Poisson coefficients sp/cp/pp/lp per level (24*msh)
+    // statistics
+    tb_poisson_stats stats;
+    // host staging for the mirrors
+    std::vector<cplx> hbuf;
+    // mixed form
+    void* mixed = nullptr;
+};
+
+// ---- host helpers (tb_host.cpp) -------------------------------------------
+int tb_host_build_tables(tb_ctx* c);            // after coefficients are known
+int tb_host_upload_baseflow(tb_ctx* c);
+double tb_powi(double x, int m);
+
+// ---- kernel launchers ------------------------------------------------------
+// Batched x-line operators (derivs_par.f:80-113, filter_par.f:144-177).
+enum XOp { XOP_D1 = 0, XOP_D2 = 1, XOP_FILTER = 2 };
+struct XJob { const cplx* src; cplx* dst; int op; };  // src and dst must not alias
+int tb_launch_xlines(tb_ctx* c, const XJob* jobs, int njobs);
+enum YOp { YOP_D1 = 0, YOP_D1FV = 1, YOP_D2 = 2 };
+struct YJob { const cplx* src; cplx* dst; int op; };
+int tb_launch_ylines(tb_ctx* c, const YJob* jobs, int njobs);
+
+int tb_launch_nlterms(tb_ctx* c, cplx* a, cplx* b, cplx* cc);
+int tb_launch_f_to_p(tb_ctx* c, double* phys, const cplx* four);
+int tb_launch_p_to_f(tb_ctx* c, cplx* four, const double* phys);
+int tb_launch_les(tb_ctx* c, cplx* fx, cplx* fy, cplx* fz);
+int tb_launch_cvirt(tb_ctx* c, cplx* fx, cplx* fy, cplx* fz, bool accumulate);
+int tb_delta_setup(tb_ctx* c);
+
+int tb_drv_k(tb_ctx* c, cplx* dvx, cplx* dvy, cplx* dvz);
+int tb_drv_forced(tb_ctx* c, cplx* dvx, cplx* dvy, cplx* dvz, cplx* f[3], cplx* df[4]);
+int tb_rk_update(tb_ctx* c, int stage);
+int tb_loop_impl(tb_ctx* c, double erro, bool filter);
+int tb_filter(tb_ctx* c);
+int tb_bzone_k(tb_ctx* c);
+int tb_bzonew_k(tb_ctx* c);
+int tb_outuy_k(tb_ctx* c, cplx* dwzdx);
+int tb_poi_ux_k(tb_ctx* c, cplx* duydy);
+int tb_poi_uz_k(tb_ctx* c, const cplx* duydy);
+int tb_wx_wall_k(tb_ctx* c, cplx* lapv);
+int tb_wz_wall_k(tb_ctx* c, const cplx* lapv);
+int tb_ts_pert_k(tb_ctx* c, int t, double tempt);
+int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro);
+int tb_poisson_setup(tb_ctx* c);
+int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro);
+int tb_mixed_setup(tb_ctx* c);
+void tb_mixed_free(tb_ctx* c);
+
+// grid helpers
+inline unsigned tb_blocks(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+inline size_t tb_n3(const tb_ctx* c) { return (size_t)c->g.nx * c->g.ny * c->g.K; }
+inline size_t tb_n2(const tb_ctx* c) { return (size_t)c->g.nx * c->g.ny; }

@@ -1,0 +1,639 @@
+// tb_poisson.cu -- multigrid v-Poisson per spanwise mode, plain FP64 form
+// (poi_uy and its helpers, poisson_par.f:6-963; band solves penta_par.f:308-404).
+//
+// The reference relaxes x-lines in lexicographic order (each y-line solve uses
+// the lines i-1, i-2 already updated in the same sweep), so within one mode
+// the lines are strictly sequential.  Here one CTA owns one mode and walks the
+// lines in the reference order.  Each y-line solve (a pentadiagonal LU whose
+// factors depend only on mode and level, factored once at set-up) is split
+// into 32 row chunks, one per lane: local recurrences with zero carry, a warp
+// scan of the 2x2 chunk propagators (precomputed), and a fix-up with
+// precomputed homogeneous responses.  Defect, restriction, correction and
+// interpolation are grid-parallel over all modes.
+#include "tb_internal.h"
+#include <cmath>
+#include <cstring>
+#include <algorithm>
+
+void tb_poisson_band_matrix(const tb_ctx* c, int type, int lvl, int k, std::vector<double>& a);
+
+namespace {
+
+constexpr int SOR_THREADS = 128;
+constexpr int SMAX = 16;  // rows per lane (ny <= 512)
+
+// Layout of one (type, level, mode) block of solve tables (doubles):
+//   [0, 5ny)          L1, L2, U1, U2, ID            (band5_poi factors)
+//   [5ny, 7ny)        h1, h2   forward homogeneous responses per row
+//   [7ny, 9ny)        k1, k2   backward homogeneous responses per row
+//   [9ny, 9ny+640)    forward scan propagators  Pf[step][lane][4]
+//   [9ny+640, +640)   backward scan propagators Pb[step][lane][4]
+__host__ __device__ inline size_t blk_size(int ny) { return (size_t)9 * ny + 1280; }
+
+struct PoiDev {
+    cplx *fc, *sc, *fct, *def;    // per-mode blocks
+    const double* tab;            // solve tables
+    const double* coef;           // sp(7) cp(8) pp(4) lp(5) per level
+    const double* qdy2;           // (ny, msh)
+    const double* k2b2;
+    int* state;                   // per mode: [2k] active, [2k+1] vcycles done
+    double* err;
+    int nx, ny, K, msh;
+    int ptsx[TB_MAX_MSH], ptsy[TB_MAX_MSH];
+    size_t off[TB_MAX_MSH], elems, dstride;
+    double dx2[TB_MAX_MSH];
+    double fac_y, alpha;
+};
+
+__device__ __forceinline__ cplx& AT(cplx* base, const PoiDev& P, int k, int l, int i, int j) {
+    return base[(size_t)k * P.elems + P.off[l] + (size_t)i + (size_t)P.ptsx[l] * j];
+}
+
+// ---------------------------------------------------------------------------
+// function_source (poisson_par.f:111-164) for all modes.
+__global__ void k_source(PoiDev P, const cplx* wx, const cplx* dwzdx, const cplx* uy, const double* duexmdx,
+                         const double* uyb, double beta, double dy, double stf_pow, int form) {
+    size_t n = (size_t)P.nx * P.ny * P.K;
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    int i = (int)(q % P.nx), j = (int)((q / P.nx) % P.ny), k = (int)(q / ((size_t)P.nx * P.ny));
+    const double* c0 = P.coef;  // level 1
+    double kb = (double)k * beta;
+    int J = P.ny;
+    auto S = [&](int jj) {
+        size_t o = (size_t)i + (size_t)P.nx * (jj + (size_t)J * k);
+        cplx w = wx[o], d = dwzdx[o];
+        return make_double2(kb * w.y - d.x, -kb * w.x - d.y);
+    };
+    cplx s;
+    if (j == 0) s = make_double2(0, 0);
+    else if (j == 1) { cplx a = S(1), b = S(2); s = make_double2(c0[1] * a.x + c0[2] * b.x, c0[1] * a.y + c0[2] * b.y); }
+    else if (j <= J - 3) {
+        cplx a = S(j - 1), b = S(j), d = S(j + 1);
+        s = make_double2(c0[7] * a.x + c0[8] * b.x + c0[9] * d.x, c0[7] * a.y + c0[8] * b.y + c0[9] * d.y);
+    } else if (j == J - 2) s = S(J - 2);
+    else {
+        s = make_double2(0, 0);
+        if ((form == 0 || form == 4) && k == 0) {
+            double dya = dy * stf_pow;
+            size_t o = (size_t)i + (size_t)P.nx * (J - 1);
+            double lp1 = c0[19], lp2 = c0[20];
+            s = make_double2(-(lp1 * dwzdx[o].x) + lp2 * duexmdx[i] / dya - lp2 * P.alpha * uyb[o] / dya / sqrt(P.fac_y),
+                             -(lp1 * dwzdx[o].y));
+        }
+    }
+    AT(P.sc, P, k, 0, i, j) = s;
+    AT(P.fc, P, k, 0, i, j) = uy[q];
+}
+
+// ---------------------------------------------------------------------------
+// One lexicographic line-relaxation pass set (sor, poisson_par.f:167-226).
+__global__ void __launch_bounds__(SOR_THREADS) k_sor(PoiDev P, int l, int itera, double rf) {
+    int k = blockIdx.x;
+    if (!P.state[2 * k]) return;
+    const int nxl = P.ptsx[l], n = P.ptsy[l];
+    extern __shared__ cplx sm[];
+    cplx* g = sm;         // x-stencil sums per row
+    cplx* r = sm + n;     // line right-hand side
+    const double* cf = P.coef + 24 * l;
+    const double sp2 = cf[1], sp3 = cf[2], cp1 = cf[7], cp2 = cf[8], cp3 = cf[9];
+    const double qx = 1.0 / (12.0 * P.dx2[l] * P.fac_y);
+    cplx* F = P.fc + (size_t)k * P.elems + P.off[l];
+    const cplx* SC = P.sc + (size_t)k * P.elems + P.off[l];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int S = max(2, (n + 31) / 32);
+    const int r0 = lane * S, r1 = min(n, r0 + S);  // lane rows [r0, r1)
+    for (int it = 0; it < itera; it++) {
+        for (int step = 0; step < nxl - 2; step++) {
+            // order: border i=2, border i=nx-1, then centre 3..nx-2 (1-based)
+            int i, type;
+            if (step == 0) { i = 1; type = 1; }
+            else if (step == 1) { i = nxl - 2; type = 1; }
+            else { i = step; type = 0; }
+            // phase A: x-stencil per row
+            for (int j = threadIdx.x; j < n; j += blockDim.x) {
+                const cplx* Fj = F + (size_t)nxl * j;
+                cplx v;
+                if (type == 0) {
+                    cplx a = Fj[i - 2], b = Fj[i - 1], c = Fj[i + 1], d = Fj[i + 2];
+                    v = make_double2(16.0 * (b.x + c.x) - (a.x + d.x), 16.0 * (b.y + c.y) - (a.y + d.y));
+                } else {
+                    int e = (i == 1) ? 1 : -1;
+                    cplx a = Fj[i - e], b = Fj[i + e], c = Fj[i + 2 * e], d = Fj[i + 3 * e], f = Fj[i + 4 * e];
+                    v = make_double2(10.0 * a.x - 4.0 * b.x + 14.0 * c.x - 6.0 * d.x + f.x,
+                                     10.0 * a.y - 4.0 * b.y + 14.0 * c.y - 6.0 * d.y + f.y);
+                }
+                g[j] = v;
+            }
+            __syncthreads();
+            // phase B: rhs rows
+            for (int j = threadIdx.x; j < n; j += blockDim.x) {
+                cplx v;
+                if (j == 0) v = F[i];
+                else {
+                    cplx s = SC[(size_t)i + (size_t)nxl * j];
+                    cplx t;
+                    if (j == 1) t = make_double2(sp3 * g[2].x + sp2 * g[1].x, sp3 * g[2].y + sp2 * g[1].y);
+                    else if (j <= n - 3)
+                        t = make_double2(cp1 * g[j - 1].x + cp2 * g[j].x + cp3 * g[j + 1].x,
+                                         cp1 * g[j - 1].y + cp2 * g[j].y + cp3 * g[j + 1].y);
+                    else t = g[j];
+                    v = make_double2(s.x - qx * t.x, s.y - qx * t.y);
+                }
+                r[j] = v;
+            }
+            __syncthreads();
+            // phase C: pentadiagonal solve by warp 0, chunked over lanes
+            if (warp == 0) {
+                const double* T = P.tab + ((((size_t)type * P.msh + l) * P.K + k) * blk_size(P.ny));
+                const double *L1 = T, *L2 = T + P.ny, *U1 = T + 2 * P.ny, *U2 = T + 3 * P.ny, *ID = T + 4 * P.ny;
+                const double *h1 = T + 5 * P.ny, *h2 = T + 6 * P.ny, *k1 = T + 7 * P.ny, *k2 = T + 8 * P.ny;
+                const double* Pf = T + 9 * P.ny;
+                const double* Pb = Pf + 640;
+                cplx y[SMAX];
+                // forward local (zero incoming)
+                cplx ym1 = make_double2(0, 0), ym2 = make_double2(0, 0);
+#pragma unroll
+                for (int s = 0; s < SMAX; s++) {
+                    int j = r0 + s;
+                    if (j < r1) {
+                        cplx v = r[j];
+                        double a1 = L1[j], a2 = L2[j];
+                        cplx yy = make_double2(v.x - a2 * ym2.x - a1 * ym1.x, v.y - a2 * ym2.y - a1 * ym1.y);
+                        y[s] = yy; ym2 = ym1; ym1 = yy;
+                    }
+                }
+                // outgoing state (y_e, y_{e-1}) with zero incoming
+                cplx b0 = ym1, b1 = ym2;
+#pragma unroll
+                for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
+                    cplx o0, o1;
+                    o0.x = __shfl_up_sync(0xffffffffu, b0.x, off); o0.y = __shfl_up_sync(0xffffffffu, b0.y, off);
+                    o1.x = __shfl_up_sync(0xffffffffu, b1.x, off); o1.y = __shfl_up_sync(0xffffffffu, b1.y, off);
+                    if (lane >= off) {
+                        const double* M = Pf + (d * 32 + lane) * 4;
+                        b0 = make_double2(b0.x + M[0] * o0.x + M[1] * o1.x, b0.y + M[0] * o0.y + M[1] * o1.y);
+                        b1 = make_double2(b1.x + M[2] * o0.x + M[3] * o1.x, b1.y + M[2] * o0.y + M[3] * o1.y);
+                    }
+                }
+                // incoming carry from the previous lane
+                cplx Y1, Y2;
+                Y1.x = __shfl_up_sync(0xffffffffu, b0.x, 1); Y1.y = __shfl_up_sync(0xffffffffu, b0.y, 1);
+                Y2.x = __shfl_up_sync(0xffffffffu, b1.x, 1); Y2.y = __shfl_up_sync(0xffffffffu, b1.y, 1);
+                if (lane == 0) { Y1 = make_double2(0, 0); Y2 = make_double2(0, 0); }
+#pragma unroll
+                for (int s = 0; s < SMAX; s++) {
+                    int j = r0 + s;
+                    if (j < r1) {
+                        double a = h1[j], b = h2[j];
+                        y[s] = make_double2(y[s].x + a * Y1.x + b * Y2.x, y[s].y + a * Y1.y + b * Y2.y);
+                    }
+                }
+                // backward local (zero incoming from the right)
+                cplx xp1 = make_double2(0, 0), xp2 = make_double2(0, 0);
+#pragma unroll
+                for (int s = SMAX - 1; s >= 0; s--) {
+                    int j = r0 + s;
+                    if (j < r1) {
+                        double u1 = U1[j], u2 = U2[j], id = ID[j];
+                        cplx xx = make_double2((y[s].x - u1 * xp1.x - u2 * xp2.x) * id, (y[s].y - u1 * xp1.y - u2 * xp2.y) * id);
+                        y[s] = xx; xp2 = xp1; xp1 = xx;
+                    }
+                }
+                // outgoing (x_s, x_{s+1}); scan from high lanes to low
+                b0 = xp1; b1 = xp2;
+#pragma unroll
+                for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
+                    cplx o0, o1;
+                    o0.x = __shfl_down_sync(0xffffffffu, b0.x, off); o0.y = __shfl_down_sync(0xffffffffu, b0.y, off);
+                    o1.x = __shfl_down_sync(0xffffffffu, b1.x, off); o1.y = __shfl_down_sync(0xffffffffu, b1.y, off);
+                    if (lane + off < 32) {
+                        const double* M = Pb + (d * 32 + lane) * 4;
+                        b0 = make_double2(b0.x + M[0] * o0.x + M[1] * o1.x, b0.y + M[0] * o0.y + M[1] * o1.y);
+                        b1 = make_double2(b1.x + M[2] * o0.x + M[3] * o1.x, b1.y + M[2] * o0.y + M[3] * o1.y);
+                    }
+                }
+                cplx X1, X2;
+                X1.x = __shfl_down_sync(0xffffffffu, b0.x, 1); X1.y = __shfl_down_sync(0xffffffffu, b0.y, 1);
+                X2.x = __shfl_down_sync(0xffffffffu, b1.x, 1); X2.y = __shfl_down_sync(0xffffffffu, b1.y, 1);
+                if (lane == 31) { X1 = make_double2(0, 0); X2 = make_double2(0, 0); }
+                // fix-up and relaxation fc += rf (x - fc), rows j >= 1
+#pragma unroll
+                for (int s = 0; s < SMAX; s++) {
+                    int j = r0 + s;
+                    if (j < r1 && j >= 1) {
+                        double a = k1[j], b = k2[j];
+                        cplx xx = make_double2(y[s].x + a * X1.x + b * X2.x, y[s].y + a * X1.y + b * X2.y);
+                        cplx& f = F[(size_t)i + (size_t)nxl * j];
+                        cplx fo = f;
+                        f = make_double2(fo.x + rf * (xx.x - fo.x), fo.y + rf * (xx.y - fo.y));
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// defect (poisson_par.f:543-793): def = sc + si * (L fc) at level l;
+// si > 0 also stores it into sc(l) (coarse right-hand side).
+__global__ void k_defect(PoiDev P, int l, double si) {
+    const int nxl = P.ptsx[l], n = P.ptsy[l];
+    size_t per = (size_t)(nxl - 2) * (n - 1);
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * P.K) return;
+    int k = (int)(q / per);
+    if (!P.state[2 * k]) return;
+    size_t rq = q % per;
+    int i = 1 + (int)(rq % (nxl - 2));
+    int j = 1 + (int)(rq / (nxl - 2));
+    const double* cf = P.coef + 24 * l;
+    const double *SPc = cf, *CPc = cf + 7, *PPc = cf + 15, *LPc = cf + 19;
+    double k2b2 = P.k2b2[k];
+    double alpha2 = sqrt((P.alpha * P.alpha - k2b2) / P.fac_y);
+    double den = 1.0 / (12.0 * P.dx2[l] * P.fac_y), ify = 1.0 / P.fac_y;
+    const cplx* F = P.fc + (size_t)k * P.elems + P.off[l];
+    auto f = [&](int ii, int jj) -> cplx { return F[(size_t)ii + (size_t)nxl * jj]; };
+    auto bx = [&](int jj) -> cplx {
+        if (i == 1 || i == nxl - 2) {
+            int e = (i == 1) ? 1 : -1;
+            cplx a = f(i - e, jj), c0 = f(i, jj), b = f(i + e, jj), c = f(i + 2 * e, jj), d = f(i + 3 * e, jj), g = f(i + 4 * e, jj);
+            return make_double2(10.0 * a.x - 15.0 * c0.x - 4.0 * b.x + 14.0 * c.x - 6.0 * d.x + g.x,
+                                10.0 * a.y - 15.0 * c0.y - 4.0 * b.y + 14.0 * c.y - 6.0 * d.y + g.y);
+        }
+        cplx a = f(i - 2, jj), b = f(i - 1, jj), c0 = f(i, jj), c = f(i + 1, jj), d = f(i + 2, jj);
+        return make_double2(-a.x + 16.0 * b.x - 30.0 * c0.x + 16.0 * c.x - d.x, -a.y + 16.0 * b.y - 30.0 * c0.y + 16.0 * c.y - d.y);
+    };
+    cplx b, cc, d;
+    double q2;
+    double top = 0.0;
+    if (j == 1) {
+        cplx b1 = bx(1), b2 = bx(2);
+        b = make_double2(SPc[2] * b2.x + SPc[1] * b1.x, SPc[2] * b2.y + SPc[1] * b1.y);
+        cplx f0 = f(i, 0), f1 = f(i, 1), f2 = f(i, 2), f3 = f(i, 3);
+        cc = make_double2(SPc[3] * f0.x + SPc[4] * f1.x + SPc[5] * f2.x + SPc[6] * f3.x,
+                          SPc[3] * f0.y + SPc[4] * f1.y + SPc[5] * f2.y + SPc[6] * f3.y);
+        d = make_double2(k2b2 * (SPc[1] * f1.x + SPc[2] * f2.x), k2b2 * (SPc[1] * f1.y + SPc[2] * f2.y));
+        q2 = P.qdy2[0 + (size_t)P.ny * l];
+    } else if (j <= n - 3) {
+        cplx ba = bx(j - 1), bb = bx(j), bc = bx(j + 1);
+        b = make_double2(CPc[0] * ba.x + CPc[1] * bb.x + CPc[2] * bc.x, CPc[0] * ba.y + CPc[1] * bb.y + CPc[2] * bc.y);
+        cplx fm2 = f(i, j - 2), fm1 = f(i, j - 1), f0 = f(i, j), fp1 = f(i, j + 1), fp2 = f(i, j + 2);
+        cc = make_double2(CPc[3] * fm2.x + CPc[4] * fm1.x + CPc[5] * f0.x + CPc[6] * fp1.x + CPc[7] * fp2.x,
+                          CPc[3] * fm2.y + CPc[4] * fm1.y + CPc[5] * f0.y + CPc[6] * fp1.y + CPc[7] * fp2.y);
+        d = make_double2(k2b2 * (CPc[0] * fm1.x + CPc[1] * f0.x + CPc[2] * fp1.x), k2b2 * (CPc[0] * fm1.y + CPc[1] * f0.y + CPc[2] * fp1.y));
+        q2 = P.qdy2[(j - 2) + (size_t)P.ny * l];
+    } else if (j == n - 2) {
+        b = bx(j);
+        cplx fm1 = f(i, j - 1), f0 = f(i, j), fp1 = f(i, j + 1);
+        cc = make_double2(PPc[3] * fp1.x + PPc[2] * f0.x + PPc[1] * fm1.x, PPc[3] * fp1.y + PPc[2] * f0.y + PPc[1] * fm1.y);
+        d = make_double2(k2b2 * f0.x, k2b2 * f0.y);
+        q2 = P.qdy2[(j - 1) + (size_t)P.ny * l];
+    } else {
+        b = bx(j);
+        cplx fm2 = f(i, j - 2), fm1 = f(i, j - 1), f0 = f(i, j);
+        cc = make_double2(LPc[2] * f0.x + LPc[3] * fm1.x + LPc[4] * fm2.x, LPc[2] * f0.y + LPc[3] * fm1.y + LPc[4] * fm2.y);
+        d = make_double2(k2b2 * f0.x, k2b2 * f0.y);
+        q2 = P.qdy2[(j - 2) + (size_t)P.ny * l];
+        top = LPc[1] * alpha2 * sqrt(q2);
+    }
+    cplx fij = f(i, j);
+    const cplx* SC = P.sc + (size_t)k * P.elems + P.off[l];
+    cplx s = SC[(size_t)i + (size_t)nxl * j];
+    cplx v = make_double2(s.x + si * (b.x * den + cc.x * q2 + d.x * ify - top * fij.x),
+                          s.y + si * (b.y * den + cc.y * q2 + d.y * ify - top * fij.y));
+    P.def[(size_t)k * P.dstride + (size_t)i + (size_t)nxl * j] = v;
+    if (si > 0) AT(P.sc, P, k, l, i, j) = v;
+}
+
+// get_max_value + verifica_poi (poisson_par.f:67-108, 945-963): per mode.
+__global__ void k_check(PoiDev P, double tol, int vcycle) {
+    int k = blockIdx.x;
+    if (!P.state[2 * k]) return;
+    const int nx = P.ptsx[0], n = P.ptsy[0];
+    const cplx* D = P.def + (size_t)k * P.dstride;
+    double m = 0.0;
+    int nonfinite = 0;
+    for (int q = threadIdx.x; q < (nx - 2) * (n - 1); q += blockDim.x) {
+        int i = 1 + q % (nx - 2), j = 1 + q / (nx - 2);
+        cplx v = D[(size_t)i + (size_t)nx * j];
+        double a = hypot(v.x, v.y);
+        if (!(a == a) || isinf(a)) nonfinite = 1;
+        m = fmax(m, a);
+    }
+    __shared__ double red[256];
+    __shared__ int bad;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    if (nonfinite) bad = 1;
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double e = bad ? __longlong_as_double(0x7ff8000000000000LL) : red[0];
+        P.err[k] = e;
+        if (bad) { P.state[2 * k] = 0; P.state[2 * k + 1] = -1 - vcycle; }
+        else if (e < tol) { P.state[2 * k] = 0; P.state[2 * k + 1] = vcycle - 1; }
+    }
+}
+
+// restrict (poisson_par.f:796-874): level l -> l+1.
+__global__ void k_restrict(PoiDev P, int l) {
+    const int nxc = P.ptsx[l + 1], nyc = P.ptsy[l + 1], nxf = P.ptsx[l], nyf = P.ptsy[l];
+    size_t per = (size_t)nxc * nyc;
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * P.K) return;
+    int k = (int)(q / per);
+    if (!P.state[2 * k]) return;
+    int i = (int)((q % per) % nxc), j = (int)((q % per) / nxc);
+    const cplx* Ff = P.fc + (size_t)k * P.elems + P.off[l];
+    const cplx* Df = P.def + (size_t)k * P.dstride;
+    auto ff = [&](int ii, int jj) { return Ff[(size_t)ii + (size_t)nxf * jj]; };
+    auto df = [&](int ii, int jj) { return Df[(size_t)ii + (size_t)nxf * jj]; };
+    int fi = 2 * i, fj = 2 * j;
+    cplx v;
+    if (j == nyc - 1) fj = nyf - 1;
+    if (i == nxc - 1) fi = nxf - 1;
+    v = ff(fi, fj);
+    AT(P.fc, P, k, l + 1, i, j) = v;
+    AT(P.fct, P, k, l + 1, i, j) = v;
+    if (i >= 1 && i <= nxc - 2) {
+        if (j >= 1 && j <= nyc - 2) {
+            cplx s = make_double2(0, 0);
+            cplx a = df(fi - 1, fj), b = df(fi + 1, fj), c = df(fi, fj - 1), d = df(fi, fj + 1), e = df(fi, fj);
+            cplx g1 = df(fi + 1, fj + 1), g2 = df(fi + 1, fj - 1), g3 = df(fi - 1, fj + 1), g4 = df(fi - 1, fj - 1);
+            s.x = 6.25e-2 * (2.0 * (a.x + b.x + c.x + d.x) + 4.0 * e.x + g1.x + g2.x + g3.x + g4.x);
+            s.y = 6.25e-2 * (2.0 * (a.y + b.y + c.y + d.y) + 4.0 * e.y + g1.y + g2.y + g3.y + g4.y);
+            AT(P.sc, P, k, l + 1, i, j) = s;
+        } else if (j == nyc - 1) {
+            cplx a = df(fi - 1, fj), e = df(fi, fj), b = df(fi + 1, fj);
+            AT(P.sc, P, k, l + 1, i, j) = make_double2(0.25 * (a.x + 2.0 * e.x + b.x), 0.25 * (a.y + 2.0 * e.y + b.y));
+        }
+    }
+}
+
+// correction (poisson_par.f:923-942) at level l (coarse).
+__global__ void k_correction(PoiDev P, int l) {
+    const int nxl = P.ptsx[l], n = P.ptsy[l];
+    size_t per = (size_t)nxl * n;
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * P.K) return;
+    int k = (int)(q / per);
+    if (!P.state[2 * k]) return;
+    int i = (int)((q % per) % nxl), j = (int)((q % per) / nxl);
+    if (i < 1 || i > nxl - 2) return;
+    cplx& f = AT(P.fc, P, k, l, i, j);
+    cplx t = AT(P.fct, P, k, l, i, j);
+    f = make_double2(f.x - t.x, f.y - t.y);
+}
+
+// intpol (poisson_par.f:877-920): add the bilinear interpolant of level l to l-1.
+__global__ void k_intpol(PoiDev P, int l) {
+    const int nxc = P.ptsx[l], nxf = P.ptsx[l - 1], nyf = P.ptsy[l - 1];
+    size_t per = (size_t)nxf * nyf;
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * P.K) return;
+    int k = (int)(q / per);
+    if (!P.state[2 * k]) return;
+    int i = (int)((q % per) % nxf), j = (int)((q % per) / nxf);
+    if (i < 1 || i > nxf - 2) return;
+    const cplx* C = P.fc + (size_t)k * P.elems + P.off[l];
+    auto cv = [&](int ci, int cj) { return C[(size_t)ci + (size_t)nxc * cj]; };
+    // temp on an odd fine row (0-based even j): coarse value or x-average
+    auto row = [&](int jj) -> cplx {
+        int cj = jj / 2;
+        if ((i & 1) == 0) return cv(i / 2, cj);
+        cplx a = cv(i / 2, cj), b = cv(i / 2 + 1, cj);
+        return make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+    };
+    cplx t;
+    if ((j & 1) == 0) t = row(j);
+    else { cplx a = row(j + 1), b = row(j - 1); t = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y)); }
+    cplx& f = AT(P.fc, P, k, l - 1, i, j);
+    f = make_double2(f.x + t.x, f.y + t.y);
+}
+
+// uy(i,j,k) = fc(i,j,1) for j >= 2, 2 <= i <= ptsx-1 (poisson_par.f:53-57).
+__global__ void k_write_uy(PoiDev P, cplx* uy) {
+    size_t n = (size_t)P.nx * P.ny * P.K;
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    int i = (int)(q % P.nx), j = (int)((q / P.nx) % P.ny), k = (int)(q / ((size_t)P.nx * P.ny));
+    if (j < 1 || i < 1 || i > P.nx - 2) return;
+    uy[q] = AT(P.fc, P, k, 0, i, j);
+}
+
+__global__ void k_activate(int* state, int K) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < K) { state[2 * k] = 1; state[2 * k + 1] = 0; }
+}
+
+PoiDev make_dev(tb_ctx* c) {
+    PoiDev P;
+    std::memset(&P, 0, sizeof P);
+    P.fc = c->pfc; P.sc = c->psc; P.fct = c->pfct; P.def = c->pdef; P.tab = c->pcarry; P.coef = c->pcoef;
+    P.qdy2 = c->pqdy2; P.k2b2 = c->k2b2; P.state = c->pstate; P.err = c->perr;
+    P.nx = c->g.nx; P.ny = c->g.ny; P.K = c->g.K; P.msh = c->g.msh;
+    for (int l = 0; l < c->g.msh; l++) {
+        P.ptsx[l] = c->g.ptsx[l]; P.ptsy[l] = c->g.ptsy[l]; P.off[l] = c->g.lvl_off[l]; P.dx2[l] = c->h_dx2[l];
+    }
+    P.elems = c->g.lvl_elems; P.dstride = (size_t)c->g.nx * c->g.ny;
+    P.fac_y = c->cfg.fac_y; P.alpha = c->cfg.alpha;
+    return P;
+}
+
+// Host: chunk tables of the line solve for one (type, level, mode).
+void chunk_tables(int n, int ny, const double* L1, const double* L2, const double* U1, const double* U2, const double* ID,
+                  double* out) {
+    int S = std::max(2, (n + 31) / 32);
+    double *h1 = out, *h2 = out + ny, *k1 = out + 2 * ny, *k2 = out + 3 * ny;
+    double* Pf = out + 4 * ny;
+    double* Pb = Pf + 640;
+    double Mf[32][4], Mb[32][4];
+    for (int t = 0; t < 32; t++) {
+        int r0 = t * S, r1 = std::min(n, r0 + S);
+        // forward: responses to incoming (Y1 = y_{r0-1}, Y2 = y_{r0-2})
+        double e0[2], e1[2];   // outgoing (y_{e}, y_{e-1}) for unit incoming
+        for (int u = 0; u < 2; u++) {
+            double ym1 = (u == 0) ? 1.0 : 0.0, ym2 = (u == 0) ? 0.0 : 1.0;
+            for (int j = r0; j < r1; j++) {
+                double y = -L2[j] * ym2 - L1[j] * ym1;
+                (u == 0 ? h1 : h2)[j] = y;
+                ym2 = ym1; ym1 = y;
+            }
+            e0[u] = ym1; e1[u] = ym2;  // for an empty chunk this is the identity
+        }
+        Mf[t][0] = e0[0]; Mf[t][1] = e0[1]; Mf[t][2] = e1[0]; Mf[t][3] = e1[1];
+        // backward: responses to incoming (X1 = x_{r1}, X2 = x_{r1+1})
+        for (int u = 0; u < 2; u++) {
+            double xp1 = (u == 0) ? 1.0 : 0.0, xp2 = (u == 0) ? 0.0 : 1.0;
+            for (int j = r1 - 1; j >= r0; j--) {
+                double x = (-U1[j] * xp1 - U2[j] * xp2) * ID[j];
+                (u == 0 ? k1 : k2)[j] = x;
+                xp2 = xp1; xp1 = x;
+            }
+            e0[u] = xp1; e1[u] = xp2;
+        }
+        Mb[t][0] = e0[0]; Mb[t][1] = e0[1]; Mb[t][2] = e1[0]; Mb[t][3] = e1[1];
+    }
+    // Kogge-Stone: A_t before each step; b_t += A_t b_{t-off}; A_t = A_t A_{t-off}
+    auto mul = [](const double* A, const double* B, double* C) {
+        double c0 = A[0] * B[0] + A[1] * B[2], c1 = A[0] * B[1] + A[1] * B[3];
+        double c2 = A[2] * B[0] + A[3] * B[2], c3 = A[2] * B[1] + A[3] * B[3];
+        C[0] = c0; C[1] = c1; C[2] = c2; C[3] = c3;
+    };
+    double Af[32][4], Ab[32][4];
+    std::memcpy(Af, Mf, sizeof Af);
+    std::memcpy(Ab, Mb, sizeof Ab);
+    for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
+        for (int t = 0; t < 32; t++) {
+            std::memcpy(Pf + (d * 32 + t) * 4, Af[t], 4 * sizeof(double));
+            std::memcpy(Pb + (d * 32 + t) * 4, Ab[t], 4 * sizeof(double));
+        }
+        double nf[32][4], nb[32][4];
+        for (int t = 0; t < 32; t++) {
+            if (t >= off) mul(Af[t], Af[t - off], nf[t]); else std::memcpy(nf[t], Af[t], sizeof nf[t]);
+            if (t + off < 32) mul(Ab[t], Ab[t + off], nb[t]); else std::memcpy(nb[t], Ab[t], sizeof nb[t]);
+        }
+        std::memcpy(Af, nf, sizeof Af);
+        std::memcpy(Ab, nb, sizeof Ab);
+    }
+}
+
+void band5_host(int n, std::vector<double>& a, double* L1, double* L2, double* U1, double* U2, double* ID) {
+    std::vector<double> al((size_t)n * 5, 0.0);
+    auto A = [&](int i, int c) -> double& { return a[(size_t)(i - 1) + (size_t)n * (c - 1)]; };
+    auto AL = [&](int i, int c) -> double& { return al[(size_t)(i - 1) + (size_t)n * (c - 1)]; };
+    const double TINY = (double)1.e-20f;
+    int m1 = 2, mm = 5, l = m1;
+    for (int i = 1; i <= m1; i++) {
+        for (int j = m1 + 2 - i; j <= mm; j++) A(i, j - l) = A(i, j);
+        l--;
+        for (int j = mm - l; j <= mm; j++) A(i, j) = 0.0;
+    }
+    l = m1;
+    for (int k = 1; k <= n; k++) {
+        double dum = A(k, 1);
+        if (l < n) l++;
+        if (dum == 0.0) A(k, 1) = TINY;
+        for (int i = k + 1; i <= l; i++) {
+            dum = A(i, 1) / A(k, 1);
+            AL(k, i - k) = dum;
+            for (int j = 2; j <= mm; j++) A(i, j - 1) = A(i, j) - dum * A(k, j);
+            A(i, mm) = 0.0;
+        }
+    }
+    for (int j = 1; j <= n; j++) {
+        L1[j - 1] = (j >= 2) ? AL(j - 1, 1) : 0.0;
+        L2[j - 1] = (j >= 3) ? AL(j - 2, 2) : 0.0;
+        U1[j - 1] = (j <= n - 1) ? A(j, 2) : 0.0;
+        U2[j - 1] = (j <= n - 2) ? A(j, 3) : 0.0;
+        ID[j - 1] = 1.0 / A(j, 1);
+    }
+}
+
+}  // namespace
+
+int tb_poisson_setup(tb_ctx* c) {
+    int ny = c->g.ny, K = c->g.K, msh = c->g.msh;
+    size_t bs = blk_size(ny);
+    std::vector<double> all((size_t)2 * msh * K * bs, 0.0), a;
+    for (int type = 0; type < 2; type++)
+        for (int l = 0; l < msh; l++)
+            for (int k = 0; k < K; k++) {
+                tb_poisson_band_matrix(c, type, l + 1, k + 1, a);
+                int n = c->g.ptsy[l];
+                double* T = &all[(((size_t)type * msh + l) * K + k) * bs];
+                band5_host(n, a, T, T + ny, T + 2 * ny, T + 3 * ny, T + 4 * ny);
+                chunk_tables(n, ny, T, T + ny, T + 2 * ny, T + 3 * ny, T + 4 * ny, T + 5 * ny);
+            }
+    if (c->pcarry) cudaFree(c->pcarry);
+    TB_CUDA(cudaMalloc(&c->pcarry, all.size() * sizeof(double)));
+    TB_CUDA(cudaMemcpy(c->pcarry, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
+    size_t w = (size_t)K * c->g.lvl_elems;
+    for (cplx** p : {&c->pfc, &c->psc, &c->pfct}) {
+        if (*p) cudaFree(*p);
+        TB_CUDA(cudaMalloc(p, w * sizeof(cplx)));
+        TB_CUDA(cudaMemset(*p, 0, w * sizeof(cplx)));
+    }
+    if (c->pdef) cudaFree(c->pdef);
+    TB_CUDA(cudaMalloc(&c->pdef, (size_t)K * c->g.nx * ny * sizeof(cplx)));
+    TB_CUDA(cudaMemset(c->pdef, 0, (size_t)K * c->g.nx * ny * sizeof(cplx)));
+    if (!c->pstate) TB_CUDA(cudaMalloc(&c->pstate, 2 * K * sizeof(int)));
+    if (!c->perr) TB_CUDA(cudaMalloc(&c->perr, K * sizeof(double)));
+    return TB_OK;
+}
+
+// poi_uy (poisson_par.f:6-64), plain FP64 form.
+int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro) {
+    PoiDev P = make_dev(c);
+    int K = c->g.K, msh = c->g.msh;
+    size_t n3 = tb_n3(c);
+    double stf_pow = tb_powi(c->cfg.stf, c->g.ny - 3);
+    k_source<<<tb_blocks(n3, 256), 256, 0, c->stream>>>(P, c->wx, dwzdx, c->uy, c->duexmdx, c->uyb, c->cfg.beta, c->cfg.dy,
+                                                         stf_pow, c->cfg.my_form);
+    TB_CHECK_LAUNCH(c);
+    k_activate<<<tb_blocks(K, 64), 64, 0, c->stream>>>(c->pstate, K);
+    TB_CHECK_LAUNCH(c);
+    std::vector<int> hs(2 * K);
+    int vmax = c->cfg.max_vcycles;
+    auto sor = [&](int l, int it, double rf) {
+        size_t smem = (size_t)2 * c->g.ptsy[l] * sizeof(cplx);
+        k_sor<<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf);
+        TB_CHECK_LAUNCH(c);
+        return TB_OK;
+    };
+    auto defect = [&](int l, double si) {
+        size_t per = (size_t)(c->g.ptsx[l] - 2) * (c->g.ptsy[l] - 1) * K;
+        k_defect<<<tb_blocks(per, 256), 256, 0, c->stream>>>(P, l, si);
+        TB_CHECK_LAUNCH(c);
+        return TB_OK;
+    };
+    int v;
+    for (v = 1; v <= vmax; v++) {
+        for (int l = 0; l < msh - 1; l++) {
+            sor(l, 3, 1.2);
+            defect(l, -1.0);
+            if (l == 0) { k_check<<<K, 256, 0, c->stream>>>(P, erro, v); TB_CHECK_LAUNCH(c); }
+            size_t per = (size_t)c->g.ptsx[l + 1] * c->g.ptsy[l + 1] * K;
+            k_restrict<<<tb_blocks(per, 256), 256, 0, c->stream>>>(P, l); TB_CHECK_LAUNCH(c);
+            defect(l + 1, 1.0);
+        }
+        sor(msh - 1, 60, 1.2);
+        for (int l = msh - 1; l >= 1; l--) {
+            size_t per = (size_t)c->g.ptsx[l] * c->g.ptsy[l] * K;
+            k_correction<<<tb_blocks(per, 256), 256, 0, c->stream>>>(P, l); TB_CHECK_LAUNCH(c);
+            size_t perf = (size_t)c->g.ptsx[l - 1] * c->g.ptsy[l - 1] * K;
+            k_intpol<<<tb_blocks(perf, 256), 256, 0, c->stream>>>(P, l); TB_CHECK_LAUNCH(c);
+            sor(l - 1, 1, 1.0);
+        }
+        TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        TB_CUDA(cudaStreamSynchronize(c->stream));
+        bool any = false;
+        for (int k = 0; k < K; k++) any = any || hs[2 * k];
+        if (!any) break;
+    }
+    k_write_uy<<<tb_blocks(n3, 256), 256, 0, c->stream>>>(P, c->uy);
+    TB_CHECK_LAUNCH(c);
+    std::vector<double> he(K);
+    TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TB_CUDA(cudaMemcpyAsync(he.data(), c->perr, K * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    TB_CUDA(cudaStreamSynchronize(c->stream));
+    c->stats.noconv = 0;
+    int nonfinite = 0;
+    for (int k = 0; k < K && k < 256; k++) {
+        int vc = hs[2 * k + 1];
+        if (hs[2 * k]) { vc = vmax; c->stats.noconv++; }
+        if (vc < 0) { nonfinite = 1; vc = -vc - 1; }
+        c->stats.vcycles[k] = vc;
+        c->stats.residual[k] = he[k];
+        c->stats.total_vcycles += vc;
+    }
+    c->stats.solves++;
+    if (nonfinite) { tb_set_error("poi_uy: non-finite defect"); return TB_ERR_NONFINITE; }
+    return TB_OK;
+}
