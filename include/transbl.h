@@ -179,6 +179,13 @@ int tb_device_field(tb_ctx* ctx, int which, void** dptr);
 int tb_stream(tb_ctx* ctx, void** stream);
 /* Kernel launches issued by this context so far (for launch accounting). */
 long long tb_launch_count(tb_ctx* ctx);
+/* CUDA-event timing of kernel families on the context stream: enable = 1
+   starts recording (and clears totals), 0 stops.  tb_profile_read returns the
+   accumulated device milliseconds and launch count of one family:
+   0 line-SOR sweeps, 1 whole poi_uy, 2 nlterms, 3 x-line batches,
+   4 y-line batches, 5 RK stages, 6 x-penta solves, 7 Poisson defects. */
+int tb_profile(tb_ctx* ctx, int enable);
+int tb_profile_read(tb_ctx* ctx, int family, double* ms, long long* launches);
 
 #ifdef __cplusplus
 }

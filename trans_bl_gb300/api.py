@@ -98,6 +98,8 @@ def load():
     lib.tb_ts_pert.argtypes = [P, C.c_int, C.c_double]
     lib.tb_device_field.argtypes = [P, C.c_int, C.POINTER(P)]
     lib.tb_stream.argtypes = [P, C.POINTER(P)]
+    lib.tb_profile.argtypes = [P, C.c_int]
+    lib.tb_profile_read.argtypes = [P, C.c_int, D, C.POINTER(C.c_longlong)]
     _lib = lib
     return lib
 
@@ -240,6 +242,17 @@ class Context:
 
     def launch_count(self):
         return int(self.lib.tb_launch_count(self.h))
+
+    PROF = {"sor": 0, "poi_uy": 1, "nlterms": 2, "xlines": 3, "ylines": 4, "stage": 5, "penta": 6, "defect": 7}
+
+    def profile(self, enable):
+        self._c(self.lib.tb_profile(self.h, 1 if enable else 0), "tb_profile")
+
+    def profile_read(self, family):
+        ms = np.zeros(1)
+        n = C.c_longlong()
+        self._c(self.lib.tb_profile_read(self.h, self.PROF[family], dptr(ms), C.byref(n)), "tb_profile_read")
+        return float(ms[0]), int(n.value)
 
     # per-subroutine mirrors -------------------------------------------------
     def _unary(self, name, f):

@@ -133,6 +133,8 @@ int tb_destroy(tb_ctx* c) {
                     c->pstate, c->perr, c->pqdy2, c->pcoef};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (int q = 0; q < 24; q++) if (c->tmp[q]) cudaFree(c->tmp[q]);
+    for (auto& r : c->prof_open) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto e : c->prof_pool) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return TB_OK;
@@ -216,6 +218,8 @@ int tb_rk_stage(tb_ctx* c, int stage, int t) {
     if (!ready(c)) return TB_ERR_STATE;
     if (stage < 1 || stage > 4) { tb_set_error("stage must be 1..4"); return TB_ERR_ARG; }
     int r;
+    cudaEvent_t ps = nullptr;
+    if ((r = tb_prof_begin(c, PROF_STAGE, &ps))) return r;
     if (stage == 1) r = tb_drv_k(c, c->dv1x, c->dv1y, c->dv1z);
     else r = tb_drv_k(c, c->dv2x, c->dv2y, c->dv2z);
     if (r) return r;
@@ -225,6 +229,7 @@ int tb_rk_stage(tb_ctx* c, int stage, int t) {
     if (stage < 4) r = tb_loop_impl(c, c->cfg.tol_stage, false);
     else r = tb_loop_impl(c, c->cfg.tol_final, true);
     if (r) return r;
+    if ((r = tb_prof_end(c, PROF_STAGE, ps))) return r;
     TB_CUDA(cudaGetLastError());
     return TB_OK;
 }
@@ -388,5 +393,31 @@ int tb_stream(tb_ctx* c, void** s) {
     return TB_OK;
 }
 long long tb_launch_count(tb_ctx* c) { return c ? c->launches : -1; }
+
+int tb_profile(tb_ctx* c, int enable) {
+    if (!c) { tb_set_error("null context"); return TB_ERR_ARG; }
+    TB_CUDA(cudaStreamSynchronize(c->stream));
+    for (auto& r : c->prof_open) { c->prof_pool.push_back(r.a); c->prof_pool.push_back(r.b); }
+    c->prof_open.clear();
+    for (int i = 0; i < 16; i++) { c->prof_ms[i] = 0; c->prof_n[i] = 0; }
+    c->prof = enable != 0;
+    return TB_OK;
+}
+int tb_profile_read(tb_ctx* c, int family, double* ms, long long* n) {
+    if (!c || family < 0 || family >= 16 || !ms || !n) { tb_set_error("bad argument"); return TB_ERR_ARG; }
+    TB_CUDA(cudaStreamSynchronize(c->stream));
+    for (auto& r : c->prof_open) {
+        float t = 0.f;
+        TB_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+        c->prof_ms[r.id] += t;
+        c->prof_n[r.id] += 1;
+        c->prof_pool.push_back(r.a);
+        c->prof_pool.push_back(r.b);
+    }
+    c->prof_open.clear();
+    *ms = c->prof_ms[family];
+    *n = c->prof_n[family];
+    return TB_OK;
+}
 
 }  // extern "C"

@@ -231,10 +231,12 @@ int tb_launch_xlines(tb_ctx* c, const XJob* jobs, int njobs) {
     bool has[3] = {false, false, false};
     for (int q = 0; q < njobs; q++) has[jobs[q].op] = true;
     unsigned nb = tb_blocks(total, 128);
+    cudaEvent_t ps = nullptr;
+    if (tb_prof_begin(c, PROF_XLINES, &ps)) return TB_ERR_CUDA;
     if (has[0]) { k_xlines<XOP_D1><<<nb, 128, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
     if (has[1]) { k_xlines<XOP_D2><<<nb, 128, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
     if (has[2]) { k_xlines<XOP_FILTER><<<nb, 128, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
-    return TB_OK;
+    return tb_prof_end(c, PROF_XLINES, ps);
 }
 
 int tb_launch_ylines(tb_ctx* c, const YJob* jobs, int njobs) {
@@ -257,8 +259,10 @@ int tb_launch_ylines(tb_ctx* c, const YJob* jobs, int njobs) {
     bool has[3] = {false, false, false};
     for (int q = 0; q < njobs; q++) has[jobs[q].op] = true;
     unsigned nb = tb_blocks(total, 128);
+    cudaEvent_t ps = nullptr;
+    if (tb_prof_begin(c, PROF_YLINES, &ps)) return TB_ERR_CUDA;
     if (has[0]) { k_ylines<YOP_D1><<<nb, 128, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
     if (has[1]) { k_ylines<YOP_D1FV><<<nb, 128, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
     if (has[2]) { k_ylines<YOP_D2><<<nb, 128, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
-    return TB_OK;
+    return tb_prof_end(c, PROF_YLINES, ps);
 }

@@ -51,6 +51,28 @@ extern "C" double tb_dt(const tb_config* c) { return (2.0 * PI) / c->omega / (do
 
 extern "C" int tb_coef_count(int msh) { return 100 + 24 * msh; }
 
+// CUDA-event brackets around a kernel family (no-ops unless tb_profile is on).
+int tb_prof_begin(tb_ctx* c, int id, cudaEvent_t* start) {
+    (void)id;
+    *start = nullptr;
+    if (!c->prof) return TB_OK;
+    cudaEvent_t e;
+    if (!c->prof_pool.empty()) { e = c->prof_pool.back(); c->prof_pool.pop_back(); }
+    else TB_CUDA(cudaEventCreate(&e));
+    TB_CUDA(cudaEventRecord(e, c->stream));
+    *start = e;
+    return TB_OK;
+}
+int tb_prof_end(tb_ctx* c, int id, cudaEvent_t start) {
+    if (!c->prof || !start) return TB_OK;
+    cudaEvent_t e;
+    if (!c->prof_pool.empty()) { e = c->prof_pool.back(); c->prof_pool.pop_back(); }
+    else TB_CUDA(cudaEventCreate(&e));
+    TB_CUDA(cudaEventRecord(e, c->stream));
+    c->prof_open.push_back(tb_ctx::ProfRec{id, start, e});
+    return TB_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Table construction (runs once per context after the coefficients are set).
 namespace {

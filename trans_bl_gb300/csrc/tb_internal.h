@@ -110,7 +110,20 @@ struct tb_ctx {
     std::vector<cplx> hbuf;
     // mixed form
     void* mixed = nullptr;
+    // optional CUDA-event timing of kernel families (tb_profile)
+    bool prof = false;
+    struct ProfRec { int id; cudaEvent_t a, b; };
+    std::vector<ProfRec> prof_open;
+    std::vector<cudaEvent_t> prof_pool;
+    double prof_ms[16] = {0};
+    long long prof_n[16] = {0};
 };
+
+// Kernel families timed by tb_profile (index into prof_ms / prof_n).
+enum ProfId { PROF_SOR = 0, PROF_POISSON = 1, PROF_NLTERMS = 2, PROF_XLINES = 3, PROF_YLINES = 4,
+              PROF_STAGE = 5, PROF_PENTA = 6, PROF_DEFECT = 7, PROF_COUNT = 8 };
+int tb_prof_begin(tb_ctx* c, int id, cudaEvent_t* start);
+int tb_prof_end(tb_ctx* c, int id, cudaEvent_t start);
 
 // ---- host helpers (tb_host.cpp) -------------------------------------------
 int tb_host_build_tables(tb_ctx* c);            // after coefficients are known

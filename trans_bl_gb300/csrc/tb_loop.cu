@@ -526,9 +526,11 @@ int tb_poi_ux_k(tb_ctx* c, cplx* duydy) {
     XJob xj[1] = {{duydy, d2, XOP_D1}};
     if ((r = tb_launch_xlines(c, xj, 1))) return r;
     PentaArgs A{d2, c->wy, c->ux, c->px.lu, c->g.nx, c->g.ny, c->g.K, 0, c->cfg.dx * c->cfg.dx, c->cfg.beta};
+    cudaEvent_t ps = nullptr;
+    if ((r = tb_prof_begin(c, PROF_PENTA, &ps))) return r;
     k_penta_x<<<tb_blocks((size_t)(c->g.ny - 1) * (c->g.K - 1), 128), 128, 0, c->stream>>>(A);
     TB_CHECK_LAUNCH(c);
-    return TB_OK;
+    return tb_prof_end(c, PROF_PENTA, ps);
 }
 int tb_poi_uz_k(tb_ctx* c, const cplx* duydy) {
     if (c->g.K < 2) return TB_OK;

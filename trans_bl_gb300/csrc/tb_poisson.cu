@@ -88,6 +88,7 @@ __global__ void k_source(PoiDev P, const cplx* wx, const cplx* dwzdx, const cplx
 
 // ---------------------------------------------------------------------------
 // One lexicographic line-relaxation pass set (sor, poisson_par.f:167-226).
+template <int S>
 __global__ void __launch_bounds__(SOR_THREADS) k_sor(PoiDev P, int l, int itera, double rf) {
     int k = blockIdx.x;
     if (!P.state[2 * k]) return;
@@ -101,8 +102,7 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor(PoiDev P, int l, int itera,
     cplx* F = P.fc + (size_t)k * P.elems + P.off[l];
     const cplx* SC = P.sc + (size_t)k * P.elems + P.off[l];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int S = max(2, (n + 31) / 32);
-    const int r0 = lane * S, r1 = min(n, r0 + S);  // lane rows [r0, r1)
+    const int r0 = lane * S, r1 = min(n, r0 + S);  // lane rows [r0, r1); S = max(2, ceil(n / 32))
     for (int it = 0; it < itera; it++) {
         for (int step = 0; step < nxl - 2; step++) {
             // order: border i=2, border i=nx-1, then centre 3..nx-2 (1-based)
@@ -150,11 +150,11 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor(PoiDev P, int l, int itera,
                 const double *h1 = T + 5 * P.ny, *h2 = T + 6 * P.ny, *k1 = T + 7 * P.ny, *k2 = T + 8 * P.ny;
                 const double* Pf = T + 9 * P.ny;
                 const double* Pb = Pf + 640;
-                cplx y[SMAX];
+                cplx y[S];
                 // forward local (zero incoming)
                 cplx ym1 = make_double2(0, 0), ym2 = make_double2(0, 0);
 #pragma unroll
-                for (int s = 0; s < SMAX; s++) {
+                for (int s = 0; s < S; s++) {
                     int j = r0 + s;
                     if (j < r1) {
                         cplx v = r[j];
@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor(PoiDev P, int l, int itera,
                 Y2.x = __shfl_up_sync(0xffffffffu, b1.x, 1); Y2.y = __shfl_up_sync(0xffffffffu, b1.y, 1);
                 if (lane == 0) { Y1 = make_double2(0, 0); Y2 = make_double2(0, 0); }
 #pragma unroll
-                for (int s = 0; s < SMAX; s++) {
+                for (int s = 0; s < S; s++) {
                     int j = r0 + s;
                     if (j < r1) {
                         double a = h1[j], b = h2[j];
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor(PoiDev P, int l, int itera,
                 // backward local (zero incoming from the right)
                 cplx xp1 = make_double2(0, 0), xp2 = make_double2(0, 0);
 #pragma unroll
-                for (int s = SMAX - 1; s >= 0; s--) {
+                for (int s = S - 1; s >= 0; s--) {
                     int j = r0 + s;
                     if (j < r1) {
                         double u1 = U1[j], u2 = U2[j], id = ID[j];
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor(PoiDev P, int l, int itera,
                 if (lane == 31) { X1 = make_double2(0, 0); X2 = make_double2(0, 0); }
                 // fix-up and relaxation fc += rf (x - fc), rows j >= 1
 #pragma unroll
-                for (int s = 0; s < SMAX; s++) {
+                for (int s = 0; s < S; s++) {
                     int j = r0 + s;
                     if (j < r1 && j >= 1) {
                         double a = k1[j], b = k2[j];
@@ -573,6 +573,8 @@ int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro) {
     PoiDev P = make_dev(c);
     int K = c->g.K, msh = c->g.msh;
     size_t n3 = tb_n3(c);
+    cudaEvent_t pall = nullptr;
+    if (tb_prof_begin(c, PROF_POISSON, &pall)) return TB_ERR_CUDA;
     double stf_pow = tb_powi(c->cfg.stf, c->g.ny - 3);
     k_source<<<tb_blocks(n3, 256), 256, 0, c->stream>>>(P, c->wx, dwzdx, c->uy, c->duexmdx, c->uyb, c->cfg.beta, c->cfg.dy,
                                                          stf_pow, c->cfg.my_form);
@@ -583,15 +585,30 @@ int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro) {
     int vmax = c->cfg.max_vcycles;
     auto sor = [&](int l, int it, double rf) {
         size_t smem = (size_t)2 * c->g.ptsy[l] * sizeof(cplx);
-        k_sor<<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf);
+        int S = std::max(2, (c->g.ptsy[l] + 31) / 32);
+        cudaEvent_t ps = nullptr;
+        if (tb_prof_begin(c, PROF_SOR, &ps)) return TB_ERR_CUDA;
+        switch (S) {
+            case 2: k_sor<2><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
+            case 3: k_sor<3><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
+            case 4: k_sor<4><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
+            case 5: k_sor<5><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
+            case 6: k_sor<6><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
+            case 7: k_sor<7><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
+            case 8: k_sor<8><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
+            case 9: k_sor<9><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
+            default: k_sor<SMAX><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
+        }
         TB_CHECK_LAUNCH(c);
-        return TB_OK;
+        return tb_prof_end(c, PROF_SOR, ps);
     };
     auto defect = [&](int l, double si) {
         size_t per = (size_t)(c->g.ptsx[l] - 2) * (c->g.ptsy[l] - 1) * K;
+        cudaEvent_t ps = nullptr;
+        if (tb_prof_begin(c, PROF_DEFECT, &ps)) return TB_ERR_CUDA;
         k_defect<<<tb_blocks(per, 256), 256, 0, c->stream>>>(P, l, si);
         TB_CHECK_LAUNCH(c);
-        return TB_OK;
+        return tb_prof_end(c, PROF_DEFECT, ps);
     };
     int v;
     for (v = 1; v <= vmax; v++) {
@@ -619,6 +636,7 @@ int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro) {
     }
     k_write_uy<<<tb_blocks(n3, 256), 256, 0, c->stream>>>(P, c->uy);
     TB_CHECK_LAUNCH(c);
+    if (tb_prof_end(c, PROF_POISSON, pall)) return TB_ERR_CUDA;
     std::vector<double> he(K);
     TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     TB_CUDA(cudaMemcpyAsync(he.data(), c->perr, K * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

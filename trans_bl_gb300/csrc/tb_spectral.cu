@@ -371,9 +371,11 @@ int tb_launch_nlterms(tb_ctx* c, cplx* a, cplx* b, cplx* cc) {
     if (r) return r;
     NlArgs A{c->ux, c->uy, c->uz, c->wx, c->wy, c->wz, a, b, cc, (int)tb_n2(c), c->g.K};
     unsigned nb = tb_blocks(A.n2, 128);
+    cudaEvent_t ps = nullptr;
+    if ((r = tb_prof_begin(c, PROF_NLTERMS, &ps))) return r;
     TB_DISPATCH_P(c->g.P, (k_nlterms<PP><<<nb, 128, 0, c->stream>>>(A)));
     TB_CHECK_LAUNCH(c);
-    return TB_OK;
+    return tb_prof_end(c, PROF_NLTERMS, ps);
 }
 
 int tb_launch_les(tb_ctx* c, cplx* fx, cplx* fy, cplx* fz) {
