@@ -187,6 +187,21 @@ long long tb_launch_count(tb_ctx* ctx);
 int tb_profile(tb_ctx* ctx, int enable);
 int tb_profile_read(tb_ctx* ctx, int family, double* ms, long long* launches);
 
+/* ---- allocation-free entry point --------------------------------------- */
+/* No counterpart in the reference: filter_trid (filter_par.f:144) on caller
+   DEVICE buffers wx, wy, wz (complex*16 (nx, ny, kfour)), for hosts that must
+   not allocate GPU memory after start-up (a memory manager that owns all free
+   device memory, or a loop under stream capture).  Needs no context and
+   allocates nothing: the filtered lines are staged in a 32 MiB array built
+   into the library, so one call takes nx*ny*kfour <= 2^21 - 4096 points and
+   nx <= 4096 (filter larger grids one slice of Fourier modes per call) and
+   returns TB_ERR_ARG beyond that.  The first call on a device sets up the
+   array's address and must precede any stream capture; calls that overlap on
+   the GPU race on the shared array.  stream is a cudaStream_t (NULL: legacy
+   default stream); the call returns once the kernels are queued. */
+int tb_filter_trid_noalloc(double* wx, double* wy, double* wz, int nx, int ny, int kfour,
+                           double alphaf, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -98,6 +98,7 @@ def load():
     lib.tb_ts_pert.argtypes = [P, C.c_int, C.c_double]
     lib.tb_device_field.argtypes = [P, C.c_int, C.POINTER(P)]
     lib.tb_stream.argtypes = [P, C.POINTER(P)]
+    lib.tb_filter_trid_noalloc.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, C.c_double, P]
     lib.tb_profile.argtypes = [P, C.c_int]
     lib.tb_profile_read.argtypes = [P, C.c_int, D, C.POINTER(C.c_longlong)]
     _lib = lib
@@ -242,6 +243,16 @@ class Context:
 
     def launch_count(self):
         return int(self.lib.tb_launch_count(self.h))
+
+    def device_field(self, which):
+        p = C.c_void_p()
+        self._c(self.lib.tb_device_field(self.h, int(which), C.byref(p)), "tb_device_field")
+        return p.value
+
+    def stream(self):
+        p = C.c_void_p()
+        self._c(self.lib.tb_stream(self.h, C.byref(p)), "tb_stream")
+        return p.value
 
     PROF = {"sor": 0, "poi_uy": 1, "nlterms": 2, "xlines": 3, "ylines": 4, "stage": 5, "penta": 6, "defect": 7}
 
