@@ -17,6 +17,12 @@ int check_cfg(const tb_config* c) {
     if (c->nx < 16 || (c->nx - 1) % step) { tb_set_error("nx-1 must be a multiple of 2^(msh-1) and nx >= 16 (main_par.f:90)"); return TB_ERR_ARG; }
     if (c->ny < (1 << msh) || c->ny < 16 || (c->ny - 1) % step) { tb_set_error("ny-1 must be a multiple of 2^(msh-1) and ny >= 2^msh (main_par.f:114-124)"); return TB_ERR_ARG; }
     if (c->ny > 512) { tb_set_error("ny > 512 not supported"); return TB_ERR_ARG; }
+    // the coarsest level's stencils reach 4 points in from each x-border and
+    // 3 rows up from the wall (coef_border, poisson_par.f:229-540)
+    if ((c->nx - 1) / step + 1 < 6 || (c->ny - 1) / step + 1 < 5) {
+        tb_set_error("the coarsest multigrid level needs >= 6 points in x and >= 5 in y; lower msh");
+        return TB_ERR_ARG;
+    }
     int P = c->kphys;
     if (P < 2 || P > 128 || (P & (P - 1))) { tb_set_error("kphys must be a power of two in [2, 128]"); return TB_ERR_ARG; }
     if (c->kfour < 1 || c->kfour > P / 2 || c->kfour > TB_MAX_K) { tb_set_error("kfour must be in [1, kphys/2]"); return TB_ERR_ARG; }
@@ -129,7 +135,7 @@ int tb_destroy(tb_ctx* c) {
                     c->gibbs, c->delta_no, c->k2b2, c->tx1.a, c->tx1.g, c->tx1.ib, c->tx2.a, c->tx2.g, c->tx2.ib,
                     c->tfil.a, c->tfil.g, c->tfil.ib, c->ty1.a, c->ty1.g, c->ty1.ib, c->tyfv.a, c->tyfv.g, c->tyfv.ib,
                     c->ty2.a, c->ty2.g, c->ty2.ib, c->ry1.w, c->ry1.off, c->ry1.cnt, c->ryfv.w, c->ryfv.off, c->ryfv.cnt,
-                    c->ry2.w, c->ry2.off, c->ry2.cnt, c->px.lu, c->pb.t, c->pfc, c->psc, c->pfct, c->pdef, c->pcarry,
+                    c->ry2.w, c->ry2.off, c->ry2.cnt, c->px.lu, c->pfc, c->psc, c->pfct, c->pdef, c->pcarry,
                     c->pstate, c->perr, c->pqdy2, c->pcoef};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (int q = 0; q < 24; q++) if (c->tmp[q]) cudaFree(c->tmp[q]);

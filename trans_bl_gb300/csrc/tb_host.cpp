@@ -167,12 +167,14 @@ void ludecomp(int n, const std::vector<double>& a, std::vector<double>& lu) {
     L(i, 3) = A(i, 3) - L(i, 2) * L(i - 1, 4) - L(i, 1) * L(i - 2, 5);
 }
 
+}  // namespace
+
 // band5_poi (penta_par.f:308-364): NR banded LU, m1 = m2 = 2, no pivoting.
 // Returns per row (0-based j): L1 = al(j-1,1), L2 = al(j-2,2), U1 = a(j,2),
 // U2 = a(j,3) and 1/a(j,1) so that
 //   y_j = r_j - L2_j y_{j-2} - L1_j y_{j-1},  x_j = (y_j - U1_j x_{j+1} - U2_j x_{j+2}) / D_j.
-void band5(int n, std::vector<double>& a /*(n,5) band, modified*/, double* L1, double* L2, double* U1, double* U2,
-           double* ID) {
+void tb_band5_factor(int n, std::vector<double>& a /*(n,5) band, modified*/, double* L1, double* L2, double* U1,
+                     double* U2, double* ID) {
     std::vector<double> al((size_t)n * 5, 0.0);
     auto A = [&](int i, int c) -> double& { return a[(size_t)(i - 1) + (size_t)n * (c - 1)]; };
     auto AL = [&](int i, int c) -> double& { return al[(size_t)(i - 1) + (size_t)n * (c - 1)]; };
@@ -204,10 +206,11 @@ void band5(int n, std::vector<double>& a /*(n,5) band, modified*/, double* L1, d
     }
 }
 
-}  // namespace
 
-// Poisson y-line matrix of coef_center / coef_border (poisson_par.f:229-340).
-void tb_poisson_band_matrix(const tb_ctx* c, int type, int lvl /*1-based*/, int k /*1-based*/, std::vector<double>& a) {
+// Poisson y-line matrix of coef_center / coef_border (poisson_par.f:229-340)
+// for y-level lvl with x-spacing^2 dx2.
+void tb_poisson_band_matrix_dx(const tb_ctx* c, int type, int lvl /*1-based*/, int k /*1-based*/, double dx2,
+                               std::vector<double>& a) {
     const tb_config& cf = c->cfg;
     int ny = c->g.ny, msh = c->g.msh;
     const double* blob = c->coefs.data();
@@ -222,7 +225,7 @@ void tb_poisson_band_matrix(const tb_ctx* c, int type, int lvl /*1-based*/, int 
     auto Q = [&](int j) { return c->h_qdy2[(size_t)(j - 1) + (size_t)ny * (lvl - 1)]; };
     int n = c->g.ptsy[lvl - 1];
     double k2b2 = c->h_k2b2[k - 1];
-    double qx = (type == 0 ? -30.0 : -15.0) / (12.0 * c->h_dx2[lvl - 1]);
+    double qx = (type == 0 ? -30.0 : -15.0) / (12.0 * dx2);
     double add = (qx + k2b2) / cf.fac_y;
     a.assign((size_t)n * 5, 0.0);
     auto A = [&](int j, int col) -> double& { return a[(size_t)(j - 1) + (size_t)n * (col - 1)]; };
@@ -247,6 +250,10 @@ void tb_poisson_band_matrix(const tb_ctx* c, int type, int lvl /*1-based*/, int 
     A(n, 2) = LP(4) * q;
     A(n, 3) = LP(3) * q + add - LP(2) * std::sqrt(q) * std::sqrt((cf.alpha * cf.alpha - k2b2) / cf.fac_y);
     (void)msh;
+}
+
+void tb_poisson_band_matrix(const tb_ctx* c, int type, int lvl /*1-based*/, int k /*1-based*/, std::vector<double>& a) {
+    tb_poisson_band_matrix_dx(c, type, lvl, k, c->h_dx2[lvl - 1], a);
 }
 
 int tb_host_build_tables(tb_ctx* c) {
@@ -362,18 +369,7 @@ int tb_host_build_tables(tb_ctx* c) {
         }
         if ((r = upload(&c->px.lu, all))) return r;
     }
-    // Poisson y-line band LU per (type, level, mode)
     {
-        std::vector<double> all((size_t)2 * msh * K * 5 * ny, 0.0), a;
-        for (int type = 0; type < 2; type++)
-            for (int l = 1; l <= msh; l++)
-                for (int k = 1; k <= K; k++) {
-                    tb_poisson_band_matrix(c, type, l, k, a);
-                    int n = g.ptsy[l - 1];
-                    double* base = &all[((((size_t)type * msh + (l - 1)) * K + (k - 1)) * 5) * ny];
-                    band5(n, a, base, base + ny, base + 2 * ny, base + 3 * ny, base + 4 * ny);
-                }
-        if ((r = upload(&c->pb.t, all))) return r;
         // Poisson coefficients per level for the device kernels: sp(7) cp(8) pp(4) lp(5)
         std::vector<double> pc((size_t)24 * msh);
         for (int l = 0; l < msh; l++) {

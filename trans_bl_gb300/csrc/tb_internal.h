@@ -52,11 +52,6 @@ struct YRhs {
 struct PentaX {
     double* lu;   // (K, 5, nx): [k][c][i], c = 0..4 -> lu(:,1..5), c = 2 holds 1/lu(:,3)
 };
-// Banded y-LU of the Poisson line operator (band5_poi) per mode, level and
-// column type (0 centre, 1 border): L1_j, L2_j, U1_j, U2_j, 1/D_j (0-based rows).
-struct PoiBand {
-    double* t;   // [type][level][k][5][ny]
-};
 
 struct TbGrid {
     int nx, ny, K, P, msh;
@@ -96,7 +91,6 @@ struct tb_ctx {
     TriLHS tx1, tx2, tfil, ty1, tyfv, ty2;
     YRhs ry1, ryfv, ry2;
     PentaX px;
-    PoiBand pb;
     // Poisson work (per mode blocks of lvl_elems complex): fc, sc, fct
     cplx *pfc = nullptr, *psc = nullptr, *pfct = nullptr, *pdef = nullptr;
     double* pcarry = nullptr;    // precomputed chunk propagators of the line solve
@@ -129,6 +123,12 @@ int tb_prof_end(tb_ctx* c, int id, cudaEvent_t start);
 int tb_host_build_tables(tb_ctx* c);            // after coefficients are known
 int tb_host_upload_baseflow(tb_ctx* c);
 double tb_powi(double x, int m);
+// Poisson y-line matrix (n, 5) of coef_center (type 0) / coef_border (type 1)
+// at y-level lvl (1-based) for mode k (1-based) with x-spacing^2 dx2.
+void tb_poisson_band_matrix(const tb_ctx* c, int type, int lvl, int k, std::vector<double>& a);
+void tb_poisson_band_matrix_dx(const tb_ctx* c, int type, int lvl, int k, double dx2, std::vector<double>& a);
+// band5_poi LU of an (n, 5) band (modified in place) into per-row L1 L2 U1 U2 1/D.
+void tb_band5_factor(int n, std::vector<double>& a, double* L1, double* L2, double* U1, double* U2, double* ID);
 
 // ---- kernel launchers ------------------------------------------------------
 // Batched x-line operators (derivs_par.f:80-113, filter_par.f:144-177).
@@ -161,6 +161,12 @@ int tb_wz_wall_k(tb_ctx* c, const cplx* lapv);
 int tb_ts_pert_k(tb_ctx* c, int t, double tempt);
 int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro);
 int tb_poisson_setup(tb_ctx* c);
+int tb_poisson_begin(tb_ctx* c, const cplx* dwzdx);
+int tb_poisson_fine_defect(tb_ctx* c);
+int tb_poisson_end(tb_ctx* c);
+void tb_chunk_tables(int n, int ny, int S, const double* L1, const double* L2, const double* U1, const double* U2,
+                     const double* ID, double* out);
+inline size_t tb_poi_blk_size(int ny) { return (size_t)9 * ny + 1280; }
 int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro);
 int tb_mixed_setup(tb_ctx* c);
 void tb_mixed_free(tb_ctx* c);

@@ -1,15 +1,855 @@
-// tb_mixed.cu -- mixed-precision form of the v-Poisson solve (placeholder
-// until the FP32 multigrid lands; selecting it is rejected at set-up).
+// tb_mixed.cu -- mixed-precision form of the v-Poisson solve (poi_uy).
+//
+// The reference solves each mode's v-Poisson problem with an FP64 FAS
+// multigrid whose smoother relaxes the y-lines in lexicographic x order
+// (poisson_par.f:6-963): every line waits for the one before it.  This form
+// keeps the reference's discrete problem and its stopping rule and changes
+// how the answer is reached:
+//
+//   outer loop, FP64 (defect correction on the reference's fine operator):
+//     d = sc - L u        -- same kernel as the plain form (poisson_par.f:543-793)
+//     stop a mode once max|d| < tol  (verifica_poi, poisson_par.f:945-963)
+//     solve L e = d       -- FP32 correction-scheme multigrid, e = 0 at start
+//     u += e
+//
+// The FP32 multigrid uses the reference's level operators (compact y-weights
+// and 4th-order x-stencils of coef_center/coef_border), full-weighting
+// restriction and bilinear prolongation on the reference's msh levels.  Below
+// them it keeps coarsening in x only (same y-level operators, dx doubled,
+// (1/4, 1/2, 1/4) restriction, linear prolongation) until a level has at most
+// DIRECT_MAX unknowns, which is solved exactly: its operator is inverted per
+// mode at set-up (FP64 Gauss-Jordan, stored in FP32) and applied as one
+// batched matrix-vector product.  The smoother relaxes y-lines in four
+// groups: the two border lines, then the centre lines by colour i mod 3.  The
+// centre stencil reaches i+-2 and the border stencil reaches 4 lines inwards,
+// so the lines of one group never read each other and a whole group is solved
+// at once, one warp per (line, mode).
+//
+// Layout: FP32 levels are stored per mode with each y-line contiguous
+// (element (i, j) of level l at off[l] + i*ptsy[l] + j), so a warp reads
+// a line and its x-neighbours with unit stride.  At 1025 x 193 x 32 modes one
+// FP32 level-0 field is 51 MB: the three FP32 arrays of the fine level fit in
+// the 129 MB L2 between sweeps.
 #include "tb_internal.h"
+#include <cmath>
+#include <cstring>
+#include <algorithm>
+#include <thread>
+
+namespace {
+
+// Relaxation sweeps before / after the coarse correction, V-cycles per FP64
+// correction, and whether the hierarchy starts with x-only coarsening
+// (until dx >= the largest y-spacing, so that y-coupling dominates at every
+// point of the coarser levels and y-line relaxation smooths everywhere).
+#ifndef TB_MG_NU_PRE
+#define TB_MG_NU_PRE 2
+#endif
+#ifndef TB_MG_NU_POST
+#define TB_MG_NU_POST 2
+#endif
+#ifndef TB_MG_INNER
+#define TB_MG_INNER 2
+#endif
+#ifndef TB_MG_SEMI_FIRST
+#define TB_MG_SEMI_FIRST 1
+#endif
+constexpr int NU_PRE = TB_MG_NU_PRE, NU_POST = TB_MG_NU_POST, INNER_VCYCLES = TB_MG_INNER;
+constexpr int RELAX_THREADS = 128;   // 4 warps, one line each
+constexpr int MG_MAX = 16;           // levels of the FP32 hierarchy
+constexpr int DIRECT_MAX = 400;      // unknowns per mode below which coarsening stops
+constexpr int DIRECT_LIMIT = 2048;   // largest directly solved level accepted
+
+struct Mixed {
+    float2 *e = nullptr, *r = nullptr, *rr = nullptr;   // per mode blocks of `elems` (line-contiguous)
+    float* tab = nullptr;     // [type][level][k] blocks of tb_poi_blk_size(ny): L1 L2 U1 U2 ID h1 h2 k1 k2 Pf Pb
+    float* coef = nullptr;    // sp(7) cp(8) pp(4) lp(5) per reference level
+    float* qdy2 = nullptr;    // (ny, msh)
+    float* ainv = nullptr;    // (K, N, N) inverse of the coarsest operator per mode
+    int NL = 0, N = 0;
+    int ptsx[MG_MAX], ptsy[MG_MAX], ylvl[MG_MAX], semi[MG_MAX], S[MG_MAX];
+    double dx2[MG_MAX];
+    size_t off[MG_MAX], elems = 0;
+};
+
+struct MgDev {
+    float2 *e, *r, *rr;
+    const float* tab;
+    const float* coef;
+    const float* qdy2;
+    const float* ainv;
+    const double* k2b2;
+    const int* state;
+    int ny, K, NL, N;
+    int ptsx[MG_MAX], ptsy[MG_MAX], ylvl[MG_MAX];
+    size_t off[MG_MAX], elems, bs;
+    float qx[MG_MAX];       // 1 / (12 dx_l^2 fac_y)
+    float ify, alpha2;      // 1 / fac_y, alpha^2
+};
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+// x-stencil of the line operator without its diagonal: centre lines
+// 16(f[i-1] + f[i+1]) - (f[i-2] + f[i+2]); border lines (i = 1, mirrored at
+// i = nxl-2) 10 f[i-1] - 4 f[i+1] + 14 f[i+2] - 6 f[i+3] + f[i+4]
+// (rhs_center / rhs_border, poisson_par.f:229-540).
+__device__ __forceinline__ float2 xsum(const float2* E, int n, int i, int j, int type, int e) {
+    auto at = [&](int ii) { return E[(size_t)n * ii + j]; };
+    if (type == 0) {
+        float2 a = at(i - 2), b = at(i - 1), c = at(i + 1), d = at(i + 2);
+        return f2(16.f * (b.x + c.x) - (a.x + d.x), 16.f * (b.y + c.y) - (a.y + d.y));
+    }
+    float2 a = at(i - e), b = at(i + e), c = at(i + 2 * e), d = at(i + 3 * e), f = at(i + 4 * e);
+    return f2(10.f * a.x - 4.f * b.x + 14.f * c.x - 6.f * d.x + f.x, 10.f * a.y - 4.f * b.y + 14.f * c.y - 6.f * d.y + f.y);
+}
+
+// Relax one group of lines at level l: lines i = first + step*t, t < nlines,
+// in every active mode; e(i, :) <- line solve of L e = r with the other lines
+// frozen.  One warp per (line, mode); the pentadiagonal solve is split into
+// 32 row chunks (local recurrences, warp scan of precomputed 2x2 chunk
+// propagators, fix-up with precomputed homogeneous responses).
+template <int S>
+__global__ void __launch_bounds__(RELAX_THREADS) k_relax(MgDev M, int l, int first, int step, int nlines) {
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * (RELAX_THREADS / 32) + wib;
+    const int k = gw / nlines;
+    if (k >= M.K || !M.state[2 * k]) return;   // uniform over the warp
+    const int i = first + step * (gw - k * nlines);
+    const int nxl = M.ptsx[l], n = M.ptsy[l];
+    const int type = (i == 1 || i == nxl - 2) ? 1 : 0, dir = (i == 1) ? 1 : -1;
+    extern __shared__ float2 smf[];
+    float2* g = smf + (size_t)wib * 2 * n;
+    float2* rs = g + n;
+    float2* E = M.e + (size_t)k * M.elems + M.off[l];
+    const float2* R = M.r + (size_t)k * M.elems + M.off[l] + (size_t)n * i;
+    for (int j = lane; j < n; j += 32) g[j] = xsum(E, n, i, j, type, dir);
+    __syncwarp();
+    const float* cf = M.coef + 24 * M.ylvl[l];
+    const float sp2 = cf[1], sp3 = cf[2], cp1 = cf[7], cp2 = cf[8], cp3 = cf[9];
+    const float qx = M.qx[l];
+    for (int j = lane; j < n; j += 32) {
+        float2 v = f2(0.f, 0.f);
+        if (j >= 1) {
+            float2 t;
+            if (j == 1) t = f2(sp3 * g[2].x + sp2 * g[1].x, sp3 * g[2].y + sp2 * g[1].y);
+            else if (j <= n - 3)
+                t = f2(cp1 * g[j - 1].x + cp2 * g[j].x + cp3 * g[j + 1].x, cp1 * g[j - 1].y + cp2 * g[j].y + cp3 * g[j + 1].y);
+            else t = g[j];
+            float2 s = R[j];
+            v = f2(s.x - qx * t.x, s.y - qx * t.y);
+        }
+        rs[j] = v;
+    }
+    __syncwarp();
+    const float* T = M.tab + (((size_t)type * M.NL + l) * M.K + k) * M.bs;
+    const int ny = M.ny;
+    const float *L1 = T, *L2 = T + ny, *U1 = T + 2 * ny, *U2 = T + 3 * ny, *ID = T + 4 * ny;
+    const float *h1 = T + 5 * ny, *h2 = T + 6 * ny, *k1 = T + 7 * ny, *k2 = T + 8 * ny;
+    const float* Pf = T + 9 * ny;
+    const float* Pb = Pf + 640;
+    const int r0 = lane * S, r1 = min(n, r0 + S);
+    float2 y[S];
+    float2 ym1 = f2(0.f, 0.f), ym2 = f2(0.f, 0.f);
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+        int j = r0 + s;
+        if (j < r1) {
+            float2 v = rs[j];
+            float a1 = L1[j], a2 = L2[j];
+            float2 yy = f2(v.x - a2 * ym2.x - a1 * ym1.x, v.y - a2 * ym2.y - a1 * ym1.y);
+            y[s] = yy; ym2 = ym1; ym1 = yy;
+        }
+    }
+    float2 b0 = ym1, b1 = ym2;
+#pragma unroll
+    for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
+        float2 o0, o1;
+        o0.x = __shfl_up_sync(0xffffffffu, b0.x, off); o0.y = __shfl_up_sync(0xffffffffu, b0.y, off);
+        o1.x = __shfl_up_sync(0xffffffffu, b1.x, off); o1.y = __shfl_up_sync(0xffffffffu, b1.y, off);
+        if (lane >= off) {
+            const float* P = Pf + (d * 32 + lane) * 4;
+            b0 = f2(b0.x + P[0] * o0.x + P[1] * o1.x, b0.y + P[0] * o0.y + P[1] * o1.y);
+            b1 = f2(b1.x + P[2] * o0.x + P[3] * o1.x, b1.y + P[2] * o0.y + P[3] * o1.y);
+        }
+    }
+    float2 Y1, Y2;
+    Y1.x = __shfl_up_sync(0xffffffffu, b0.x, 1); Y1.y = __shfl_up_sync(0xffffffffu, b0.y, 1);
+    Y2.x = __shfl_up_sync(0xffffffffu, b1.x, 1); Y2.y = __shfl_up_sync(0xffffffffu, b1.y, 1);
+    if (lane == 0) { Y1 = f2(0.f, 0.f); Y2 = f2(0.f, 0.f); }
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+        int j = r0 + s;
+        if (j < r1) y[s] = f2(y[s].x + h1[j] * Y1.x + h2[j] * Y2.x, y[s].y + h1[j] * Y1.y + h2[j] * Y2.y);
+    }
+    float2 xp1 = f2(0.f, 0.f), xp2 = f2(0.f, 0.f);
+#pragma unroll
+    for (int s = S - 1; s >= 0; s--) {
+        int j = r0 + s;
+        if (j < r1) {
+            float u1 = U1[j], u2 = U2[j], id = ID[j];
+            float2 xx = f2((y[s].x - u1 * xp1.x - u2 * xp2.x) * id, (y[s].y - u1 * xp1.y - u2 * xp2.y) * id);
+            y[s] = xx; xp2 = xp1; xp1 = xx;
+        }
+    }
+    b0 = xp1; b1 = xp2;
+#pragma unroll
+    for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
+        float2 o0, o1;
+        o0.x = __shfl_down_sync(0xffffffffu, b0.x, off); o0.y = __shfl_down_sync(0xffffffffu, b0.y, off);
+        o1.x = __shfl_down_sync(0xffffffffu, b1.x, off); o1.y = __shfl_down_sync(0xffffffffu, b1.y, off);
+        if (lane + off < 32) {
+            const float* P = Pb + (d * 32 + lane) * 4;
+            b0 = f2(b0.x + P[0] * o0.x + P[1] * o1.x, b0.y + P[0] * o0.y + P[1] * o1.y);
+            b1 = f2(b1.x + P[2] * o0.x + P[3] * o1.x, b1.y + P[2] * o0.y + P[3] * o1.y);
+        }
+    }
+    float2 X1, X2;
+    X1.x = __shfl_down_sync(0xffffffffu, b0.x, 1); X1.y = __shfl_down_sync(0xffffffffu, b0.y, 1);
+    X2.x = __shfl_down_sync(0xffffffffu, b1.x, 1); X2.y = __shfl_down_sync(0xffffffffu, b1.y, 1);
+    if (lane == 31) { X1 = f2(0.f, 0.f); X2 = f2(0.f, 0.f); }
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+        int j = r0 + s;
+        if (j < r1) rs[j] = f2(y[s].x + k1[j] * X1.x + k2[j] * X2.x, y[s].y + k1[j] * X1.y + k2[j] * X2.y);
+    }
+    __syncwarp();
+    float2* Ei = E + (size_t)n * i;
+    for (int j = lane; j < n; j += 32)
+        if (j >= 1) Ei[j] = rs[j];
+}
+
+// FP32 residual rr = r - L e at level l (interior columns, rows >= 1):
+// the operator of defect (poisson_par.f:543-793) on the line-contiguous layout.
+__global__ void k_resid(MgDev M, int l) {
+    const int nxl = M.ptsx[l], n = M.ptsy[l];
+    size_t per = (size_t)(nxl - 2) * (n - 1);
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * M.K) return;
+    int k = (int)(q / per);
+    if (!M.state[2 * k]) return;
+    size_t rq = q % per;
+    int j = 1 + (int)(rq % (n - 1)), i = 1 + (int)(rq / (n - 1));
+    const int yl = M.ylvl[l];
+    const float* cf = M.coef + 24 * yl;
+    const float *SP = cf, *CP = cf + 7, *PP = cf + 15, *LP = cf + 19;
+    const float* Q2 = M.qdy2 + (size_t)M.ny * yl;
+    const float k2b2 = (float)M.k2b2[k];
+    const float den = M.qx[l];
+    const float2* E = M.e + (size_t)k * M.elems + M.off[l];
+    auto f = [&](int ii, int jj) -> float2 { return E[(size_t)n * ii + jj]; };
+    auto bx = [&](int jj) -> float2 {
+        if (i == 1 || i == nxl - 2) {
+            int e = (i == 1) ? 1 : -1;
+            float2 a = f(i - e, jj), c0 = f(i, jj), b = f(i + e, jj), c = f(i + 2 * e, jj), d = f(i + 3 * e, jj), g = f(i + 4 * e, jj);
+            return f2(10.f * a.x - 15.f * c0.x - 4.f * b.x + 14.f * c.x - 6.f * d.x + g.x,
+                      10.f * a.y - 15.f * c0.y - 4.f * b.y + 14.f * c.y - 6.f * d.y + g.y);
+        }
+        float2 a = f(i - 2, jj), b = f(i - 1, jj), c0 = f(i, jj), c = f(i + 1, jj), d = f(i + 2, jj);
+        return f2(-a.x + 16.f * b.x - 30.f * c0.x + 16.f * c.x - d.x, -a.y + 16.f * b.y - 30.f * c0.y + 16.f * c.y - d.y);
+    };
+    float2 b, cc, d;
+    float q2, top = 0.f;
+    if (j == 1) {
+        float2 b1 = bx(1), b2 = bx(2);
+        b = f2(SP[2] * b2.x + SP[1] * b1.x, SP[2] * b2.y + SP[1] * b1.y);
+        float2 g0 = f(i, 0), g1 = f(i, 1), g2 = f(i, 2), g3 = f(i, 3);
+        cc = f2(SP[3] * g0.x + SP[4] * g1.x + SP[5] * g2.x + SP[6] * g3.x, SP[3] * g0.y + SP[4] * g1.y + SP[5] * g2.y + SP[6] * g3.y);
+        d = f2(k2b2 * (SP[1] * g1.x + SP[2] * g2.x), k2b2 * (SP[1] * g1.y + SP[2] * g2.y));
+        q2 = Q2[0];
+    } else if (j <= n - 3) {
+        float2 ba = bx(j - 1), bb = bx(j), bc = bx(j + 1);
+        b = f2(CP[0] * ba.x + CP[1] * bb.x + CP[2] * bc.x, CP[0] * ba.y + CP[1] * bb.y + CP[2] * bc.y);
+        float2 fm2 = f(i, j - 2), fm1 = f(i, j - 1), g0 = f(i, j), fp1 = f(i, j + 1), fp2 = f(i, j + 2);
+        cc = f2(CP[3] * fm2.x + CP[4] * fm1.x + CP[5] * g0.x + CP[6] * fp1.x + CP[7] * fp2.x,
+                CP[3] * fm2.y + CP[4] * fm1.y + CP[5] * g0.y + CP[6] * fp1.y + CP[7] * fp2.y);
+        d = f2(k2b2 * (CP[0] * fm1.x + CP[1] * g0.x + CP[2] * fp1.x), k2b2 * (CP[0] * fm1.y + CP[1] * g0.y + CP[2] * fp1.y));
+        q2 = Q2[j - 2];
+    } else if (j == n - 2) {
+        b = bx(j);
+        float2 fm1 = f(i, j - 1), g0 = f(i, j), fp1 = f(i, j + 1);
+        cc = f2(PP[3] * fp1.x + PP[2] * g0.x + PP[1] * fm1.x, PP[3] * fp1.y + PP[2] * g0.y + PP[1] * fm1.y);
+        d = f2(k2b2 * g0.x, k2b2 * g0.y);
+        q2 = Q2[j - 1];
+    } else {
+        b = bx(j);
+        float2 fm2 = f(i, j - 2), fm1 = f(i, j - 1), g0 = f(i, j);
+        cc = f2(LP[2] * g0.x + LP[3] * fm1.x + LP[4] * fm2.x, LP[2] * g0.y + LP[3] * fm1.y + LP[4] * fm2.y);
+        d = f2(k2b2 * g0.x, k2b2 * g0.y);
+        q2 = Q2[j - 2];
+        top = LP[1] * sqrtf((M.alpha2 - k2b2) * M.ify) * sqrtf(q2);
+    }
+    float2 fij = f(i, j);
+    size_t o = (size_t)k * M.elems + M.off[l] + (size_t)n * i + j;
+    float2 s = M.r[o];
+    M.rr[o] = f2(s.x - (b.x * den + cc.x * q2 + d.x * M.ify - top * fij.x),
+                 s.y - (b.y * den + cc.y * q2 + d.y * M.ify - top * fij.y));
+}
+
+// Full-weighting restriction of rr(l) into r(l+1) with the weights of
+// restrict (poisson_par.f:796-874); the coarse correction e(l+1) starts at 0.
+__global__ void k_restrict32(MgDev M, int l) {
+    const int nxc = M.ptsx[l + 1], nyc = M.ptsy[l + 1], nyf = M.ptsy[l];
+    size_t per = (size_t)nxc * nyc;
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * M.K) return;
+    int k = (int)(q / per);
+    if (!M.state[2 * k]) return;
+    int j = (int)((q % per) % nyc), i = (int)((q % per) / nyc);
+    size_t oc = (size_t)k * M.elems + M.off[l + 1] + (size_t)nyc * i + j;
+    M.e[oc] = f2(0.f, 0.f);
+    float2 v = f2(0.f, 0.f);
+    if (i >= 1 && i <= nxc - 2 && j >= 1) {
+        const float2* D = M.rr + (size_t)k * M.elems + M.off[l];
+        auto df = [&](int ii, int jj) { return D[(size_t)nyf * ii + jj]; };
+        int fi = 2 * i, fj = 2 * j;
+        if (j <= nyc - 2) {
+            float2 a = df(fi - 1, fj), b = df(fi + 1, fj), c = df(fi, fj - 1), d = df(fi, fj + 1), e = df(fi, fj);
+            float2 g1 = df(fi + 1, fj + 1), g2 = df(fi + 1, fj - 1), g3 = df(fi - 1, fj + 1), g4 = df(fi - 1, fj - 1);
+            v.x = 0.0625f * (2.f * (a.x + b.x + c.x + d.x) + 4.f * e.x + g1.x + g2.x + g3.x + g4.x);
+            v.y = 0.0625f * (2.f * (a.y + b.y + c.y + d.y) + 4.f * e.y + g1.y + g2.y + g3.y + g4.y);
+        } else {
+            fj = nyf - 1;
+            float2 a = df(fi - 1, fj), e = df(fi, fj), b = df(fi + 1, fj);
+            v = f2(0.25f * (a.x + 2.f * e.x + b.x), 0.25f * (a.y + 2.f * e.y + b.y));
+        }
+    }
+    M.r[oc] = v;
+}
+
+// Bilinear prolongation of e(l) added to e(l-1) (intpol, poisson_par.f:877-920).
+__global__ void k_prolong32(MgDev M, int l) {
+    const int nyc = M.ptsy[l], nxf = M.ptsx[l - 1], nyf = M.ptsy[l - 1];
+    size_t per = (size_t)nxf * nyf;
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * M.K) return;
+    int k = (int)(q / per);
+    if (!M.state[2 * k]) return;
+    int j = (int)((q % per) % nyf), i = (int)((q % per) / nyf);
+    if (i < 1 || i > nxf - 2 || j < 1) return;
+    const float2* C = M.e + (size_t)k * M.elems + M.off[l];
+    auto cv = [&](int ci, int cj) { return C[(size_t)nyc * ci + cj]; };
+    auto row = [&](int jj) -> float2 {
+        int cj = jj / 2;
+        if ((i & 1) == 0) return cv(i / 2, cj);
+        float2 a = cv(i / 2, cj), b = cv(i / 2 + 1, cj);
+        return f2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
+    };
+    float2 t;
+    if ((j & 1) == 0) t = row(j);
+    else { float2 a = row(j + 1), b = row(j - 1); t = f2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y)); }
+    float2& fe = M.e[(size_t)k * M.elems + M.off[l - 1] + (size_t)nyf * i + j];
+    fe = f2(fe.x + t.x, fe.y + t.y);
+}
+
+// x-only restriction of rr(l) into r(l+1), weights (1/4, 1/2, 1/4) in x;
+// the coarse correction e(l+1) starts at 0.
+__global__ void k_restrict_x(MgDev M, int l) {
+    const int nxc = M.ptsx[l + 1], n = M.ptsy[l + 1];
+    size_t per = (size_t)nxc * n;
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * M.K) return;
+    int k = (int)(q / per);
+    if (!M.state[2 * k]) return;
+    int j = (int)((q % per) % n), i = (int)((q % per) / n);
+    size_t oc = (size_t)k * M.elems + M.off[l + 1] + (size_t)n * i + j;
+    M.e[oc] = f2(0.f, 0.f);
+    float2 v = f2(0.f, 0.f);
+    if (i >= 1 && i <= nxc - 2 && j >= 1) {
+        const float2* D = M.rr + (size_t)k * M.elems + M.off[l] + j;
+        float2 a = D[(size_t)n * (2 * i - 1)], b = D[(size_t)n * (2 * i)], c = D[(size_t)n * (2 * i + 1)];
+        v = f2(0.25f * (a.x + 2.f * b.x + c.x), 0.25f * (a.y + 2.f * b.y + c.y));
+    }
+    M.r[oc] = v;
+}
+
+// Linear prolongation in x of e(l) added to e(l-1).
+__global__ void k_prolong_x(MgDev M, int l) {
+    const int nxf = M.ptsx[l - 1], n = M.ptsy[l - 1];
+    size_t per = (size_t)nxf * n;
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * M.K) return;
+    int k = (int)(q / per);
+    if (!M.state[2 * k]) return;
+    int j = (int)((q % per) % n), i = (int)((q % per) / n);
+    if (i < 1 || i > nxf - 2 || j < 1) return;
+    const float2* C = M.e + (size_t)k * M.elems + M.off[l] + j;
+    float2 t;
+    if ((i & 1) == 0) t = C[(size_t)n * (i / 2)];
+    else {
+        float2 a = C[(size_t)n * (i / 2)], b = C[(size_t)n * (i / 2 + 1)];
+        t = f2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
+    }
+    float2& fe = M.e[(size_t)k * M.elems + M.off[l - 1] + (size_t)n * i + j];
+    fe = f2(fe.x + t.x, fe.y + t.y);
+}
+
+// Exact solve on the coarsest level: e = A_k^{-1} r, one warp per (mode, row).
+// Unknown q is the interior point (1 + q / (n-1), 1 + q % (n-1)).
+__global__ void k_direct(MgDev M) {
+    const int lane = threadIdx.x & 31;
+    const long gw = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int N = M.N;
+    const int k = (int)(gw / N);
+    if (k >= M.K || !M.state[2 * k]) return;
+    const int p = (int)(gw - (long)k * N);
+    const int l = M.NL - 1, n = M.ptsy[l], m = n - 1;
+    const float* A = M.ainv + ((size_t)k * N + p) * N;
+    const float2* R = M.r + (size_t)k * M.elems + M.off[l];
+    float ax = 0.f, ay = 0.f;
+    for (int q = lane; q < N; q += 32) {
+        float a = A[q];
+        float2 v = R[(size_t)n * (1 + q / m) + 1 + q % m];
+        ax = fmaf(a, v.x, ax);
+        ay = fmaf(a, v.y, ay);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, o);
+        ay += __shfl_xor_sync(0xffffffffu, ay, o);
+    }
+    if (lane == 0) M.e[(size_t)k * M.elems + M.off[l] + (size_t)n * (1 + p / m) + 1 + p % m] = f2(ax, ay);
+}
+
+// FP64 defect (x-contiguous) -> FP32 right-hand side r(0) (line-contiguous)
+// through a 32x32 shared-memory tile; e(0) = 0.
+__global__ void k_seed(MgDev M, const cplx* def, int nx, int ny) {
+    __shared__ float2 tile[32][33];
+    const int k = blockIdx.z;
+    if (!M.state[2 * k]) return;   // uniform over the block
+    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        int i = i0 + threadIdx.x, j = j0 + r;
+        float2 v = f2(0.f, 0.f);
+        if (i >= 1 && i <= nx - 2 && j >= 1 && j < ny) {
+            cplx d = def[(size_t)k * nx * ny + (size_t)i + (size_t)nx * j];
+            v = f2((float)d.x, (float)d.y);
+        }
+        tile[r][threadIdx.x] = v;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        int i = i0 + r, j = j0 + threadIdx.x;
+        if (i < nx && j < ny) {
+            size_t o = (size_t)k * M.elems + M.off[0] + (size_t)ny * i + j;
+            M.r[o] = tile[threadIdx.x][r];
+            M.e[o] = f2(0.f, 0.f);
+        }
+    }
+}
+
+// u += e on the interior of the FP64 fine level (fc layout: x-contiguous).
+__global__ void k_apply(MgDev M, cplx* fc, size_t elems64, int nx, int ny) {
+    __shared__ float2 tile[32][33];
+    const int k = blockIdx.z;
+    if (!M.state[2 * k]) return;
+    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        int i = i0 + r, j = j0 + threadIdx.x;
+        float2 v = f2(0.f, 0.f);
+        if (i < nx && j < ny) v = M.e[(size_t)k * M.elems + M.off[0] + (size_t)ny * i + j];
+        tile[threadIdx.x][r] = v;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        int i = i0 + threadIdx.x, j = j0 + r;
+        if (i >= 1 && i <= nx - 2 && j >= 1 && j < ny) {
+            float2 e = tile[r][threadIdx.x];
+            cplx& u = fc[(size_t)k * elems64 + (size_t)i + (size_t)nx * j];
+            u = make_double2(u.x + (double)e.x, u.y + (double)e.y);
+        }
+    }
+}
+
+// Per-mode test of the FP64 defect (max |d| over the interior, as
+// get_max_value/verifica_poi): converged modes leave the active set with
+// the number of corrections applied; a non-finite defect stops the mode
+// with -1 - corrections.
+__global__ void k_check_mixed(const cplx* def, int* state, double* err, int nx, int ny, double tol, int it, int last) {
+    int k = blockIdx.x;
+    if (!state[2 * k]) return;
+    const cplx* D = def + (size_t)k * nx * ny;
+    double m = 0.0;
+    int bad = 0;
+    for (int q = threadIdx.x; q < (nx - 2) * (ny - 1); q += blockDim.x) {
+        int i = 1 + q % (nx - 2), j = 1 + q / (nx - 2);
+        cplx v = D[(size_t)i + (size_t)nx * j];
+        double a = hypot(v.x, v.y);
+        if (!(a == a) || isinf(a)) bad = 1;
+        m = fmax(m, a);
+    }
+    __shared__ double red[256];
+    __shared__ int sbad;
+    if (threadIdx.x == 0) sbad = 0;
+    __syncthreads();
+    if (bad) sbad = 1;
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        err[k] = sbad ? __longlong_as_double(0x7ff8000000000000LL) : red[0];
+        if (sbad) { state[2 * k] = 0; state[2 * k + 1] = -1 - it; }
+        else if (red[0] < tol) { state[2 * k] = 0; state[2 * k + 1] = it; }
+        else if (last) state[2 * k + 1] = it;   // stays active: not converged
+    }
+}
+
+Mixed* get(tb_ctx* c) { return static_cast<Mixed*>(c->mixed); }
+
+MgDev make(tb_ctx* c) {
+    Mixed* m = get(c);
+    MgDev M;
+    std::memset(&M, 0, sizeof M);
+    M.e = m->e; M.r = m->r; M.rr = m->rr; M.tab = m->tab; M.coef = m->coef; M.qdy2 = m->qdy2; M.ainv = m->ainv;
+    M.k2b2 = c->k2b2; M.state = c->pstate;
+    M.ny = c->g.ny; M.K = c->g.K; M.NL = m->NL; M.N = m->N;
+    for (int l = 0; l < m->NL; l++) {
+        M.ptsx[l] = m->ptsx[l]; M.ptsy[l] = m->ptsy[l]; M.ylvl[l] = m->ylvl[l]; M.off[l] = m->off[l];
+        M.qx[l] = (float)(1.0 / (12.0 * m->dx2[l] * c->cfg.fac_y));
+    }
+    M.elems = m->elems;
+    M.bs = tb_poi_blk_size(c->g.ny);
+    M.ify = (float)(1.0 / c->cfg.fac_y);
+    M.alpha2 = (float)(c->cfg.alpha * c->cfg.alpha);
+    return M;
+}
+
+// Rows per lane of the line solve: the smallest instantiated S with 32 S >= n.
+int pick_S(int n) {
+    static const int opts[] = {2, 3, 4, 5, 6, 7, 8, 10, 12, 16};
+    for (int s : opts)
+        if (32 * s >= n) return s;
+    return 16;
+}
+
+template <class T>
+int upl(T** d, const std::vector<T>& h) {
+    if (*d) cudaFree(*d);
+    *d = nullptr;
+    TB_CUDA(cudaMalloc((void**)d, h.size() * sizeof(T)));
+    TB_CUDA(cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return TB_OK;
+}
+
+// The level operator L (defect, poisson_par.f:543-793) at interior point
+// (i, j) of a level with nxl x n points, applied to u (line-contiguous), FP64.
+struct HostOp {
+    const double *SP, *CP, *PP, *LP, *Q2;
+    double den, ify, k2b2, topc;
+    int nxl, n;
+    double apply(const std::vector<double>& u, int i, int j) const {
+        auto f = [&](int ii, int jj) { return u[(size_t)n * ii + jj]; };
+        auto bx = [&](int jj) {
+            if (i == 1 || i == nxl - 2) {
+                int e = (i == 1) ? 1 : -1;
+                return 10.0 * f(i - e, jj) - 15.0 * f(i, jj) - 4.0 * f(i + e, jj) + 14.0 * f(i + 2 * e, jj) -
+                       6.0 * f(i + 3 * e, jj) + f(i + 4 * e, jj);
+            }
+            return -f(i - 2, jj) + 16.0 * f(i - 1, jj) - 30.0 * f(i, jj) + 16.0 * f(i + 1, jj) - f(i + 2, jj);
+        };
+        double b, cc, d, q2, top = 0.0;
+        if (j == 1) {
+            b = SP[2] * bx(2) + SP[1] * bx(1);
+            cc = SP[3] * f(i, 0) + SP[4] * f(i, 1) + SP[5] * f(i, 2) + SP[6] * f(i, 3);
+            d = k2b2 * (SP[1] * f(i, 1) + SP[2] * f(i, 2));
+            q2 = Q2[0];
+        } else if (j <= n - 3) {
+            b = CP[0] * bx(j - 1) + CP[1] * bx(j) + CP[2] * bx(j + 1);
+            cc = CP[3] * f(i, j - 2) + CP[4] * f(i, j - 1) + CP[5] * f(i, j) + CP[6] * f(i, j + 1) + CP[7] * f(i, j + 2);
+            d = k2b2 * (CP[0] * f(i, j - 1) + CP[1] * f(i, j) + CP[2] * f(i, j + 1));
+            q2 = Q2[j - 2];
+        } else if (j == n - 2) {
+            b = bx(j);
+            cc = PP[3] * f(i, j + 1) + PP[2] * f(i, j) + PP[1] * f(i, j - 1);
+            d = k2b2 * f(i, j);
+            q2 = Q2[j - 1];
+        } else {
+            b = bx(j);
+            cc = LP[2] * f(i, j) + LP[3] * f(i, j - 1) + LP[4] * f(i, j - 2);
+            d = k2b2 * f(i, j);
+            q2 = Q2[j - 2];
+            top = LP[1] * topc * std::sqrt(q2);
+        }
+        return b * den + cc * q2 + d * ify - top * f(i, j);
+    }
+};
+
+// Inverse of the coarsest-level operator of one mode (N x N, row-major),
+// by Gauss-Jordan elimination with partial pivoting in FP64.
+bool coarse_inverse(const HostOp& op, int N, float* out) {
+    const int nxl = op.nxl, n = op.n, m = n - 1;
+    std::vector<double> A((size_t)N * N, 0.0), X((size_t)N * N, 0.0), u((size_t)nxl * n, 0.0);
+    for (int q = 0; q < N; q++) {
+        int iq = 1 + q / m, jq = 1 + q % m;
+        u[(size_t)n * iq + jq] = 1.0;
+        for (int i = std::max(1, iq - 4); i <= std::min(nxl - 2, iq + 4); i++)
+            for (int j = std::max(1, jq - 3); j <= std::min(n - 1, jq + 3); j++)
+                A[(size_t)((i - 1) * m + (j - 1)) * N + q] = op.apply(u, i, j);
+        u[(size_t)n * iq + jq] = 0.0;
+    }
+    for (int p = 0; p < N; p++) X[(size_t)p * N + p] = 1.0;
+    for (int c = 0; c < N; c++) {
+        int piv = c;
+        for (int p = c + 1; p < N; p++)
+            if (std::fabs(A[(size_t)p * N + c]) > std::fabs(A[(size_t)piv * N + c])) piv = p;
+        if (A[(size_t)piv * N + c] == 0.0) return false;
+        if (piv != c)
+            for (int q = 0; q < N; q++) {
+                std::swap(A[(size_t)piv * N + q], A[(size_t)c * N + q]);
+                std::swap(X[(size_t)piv * N + q], X[(size_t)c * N + q]);
+            }
+        double inv = 1.0 / A[(size_t)c * N + c];
+        for (int q = 0; q < N; q++) { A[(size_t)c * N + q] *= inv; X[(size_t)c * N + q] *= inv; }
+        for (int p = 0; p < N; p++) {
+            if (p == c) continue;
+            double f = A[(size_t)p * N + c];
+            if (f == 0.0) continue;
+            for (int q = 0; q < N; q++) {
+                A[(size_t)p * N + q] -= f * A[(size_t)c * N + q];
+                X[(size_t)p * N + q] -= f * X[(size_t)c * N + q];
+            }
+        }
+    }
+    for (size_t q = 0; q < X.size(); q++) out[q] = (float)X[q];
+    return true;
+}
+
+int launch_relax(tb_ctx* c, const MgDev& M, int S, int l, int first, int step, int nlines) {
+    int nw = nlines * c->g.K;
+    unsigned nb = tb_blocks((size_t)nw, RELAX_THREADS / 32);
+    size_t smem = (size_t)(RELAX_THREADS / 32) * 2 * M.ptsy[l] * sizeof(float2);
+    cudaStream_t st = c->stream;
+    switch (S) {
+        case 2: k_relax<2><<<nb, RELAX_THREADS, smem, st>>>(M, l, first, step, nlines); break;
+        case 3: k_relax<3><<<nb, RELAX_THREADS, smem, st>>>(M, l, first, step, nlines); break;
+        case 4: k_relax<4><<<nb, RELAX_THREADS, smem, st>>>(M, l, first, step, nlines); break;
+        case 5: k_relax<5><<<nb, RELAX_THREADS, smem, st>>>(M, l, first, step, nlines); break;
+        case 6: k_relax<6><<<nb, RELAX_THREADS, smem, st>>>(M, l, first, step, nlines); break;
+        case 7: k_relax<7><<<nb, RELAX_THREADS, smem, st>>>(M, l, first, step, nlines); break;
+        case 8: k_relax<8><<<nb, RELAX_THREADS, smem, st>>>(M, l, first, step, nlines); break;
+        case 10: k_relax<10><<<nb, RELAX_THREADS, smem, st>>>(M, l, first, step, nlines); break;
+        case 12: k_relax<12><<<nb, RELAX_THREADS, smem, st>>>(M, l, first, step, nlines); break;
+        default: k_relax<16><<<nb, RELAX_THREADS, smem, st>>>(M, l, first, step, nlines); break;
+    }
+    TB_CHECK_LAUNCH(c);
+    return TB_OK;
+}
+
+// One relaxation sweep at level l: border lines, then centre colours 0, 1, 2.
+int sweep(tb_ctx* c, const MgDev& M, int l) {
+    Mixed* m = get(c);
+    int nxl = m->ptsx[l], r;
+    cudaEvent_t ps = nullptr;
+    if ((r = tb_prof_begin(c, PROF_SOR, &ps))) return r;
+    if ((r = launch_relax(c, M, m->S[l], l, 1, nxl - 3, 2))) return r;
+    for (int col = 0; col < 3; col++) {
+        int first = 2 + col;
+        if (first > nxl - 3) break;
+        int nl = (nxl - 3 - first) / 3 + 1;
+        if ((r = launch_relax(c, M, m->S[l], l, first, 3, nl))) return r;
+    }
+    return tb_prof_end(c, PROF_SOR, ps);
+}
+
+int vcycle(tb_ctx* c, const MgDev& M) {
+    Mixed* m = get(c);
+    const int K = c->g.K, NL = m->NL;
+    int r;
+    for (int l = 0; l < NL - 1; l++) {
+        for (int s = 0; s < NU_PRE; s++)
+            if ((r = sweep(c, M, l))) return r;
+        size_t per = (size_t)(m->ptsx[l] - 2) * (m->ptsy[l] - 1) * K;
+        k_resid<<<tb_blocks(per, 256), 256, 0, c->stream>>>(M, l);
+        TB_CHECK_LAUNCH(c);
+        size_t pc = (size_t)m->ptsx[l + 1] * m->ptsy[l + 1] * K;
+        if (m->semi[l]) k_restrict_x<<<tb_blocks(pc, 256), 256, 0, c->stream>>>(M, l);
+        else k_restrict32<<<tb_blocks(pc, 256), 256, 0, c->stream>>>(M, l);
+        TB_CHECK_LAUNCH(c);
+    }
+    k_direct<<<tb_blocks((size_t)K * m->N, 8), 256, 0, c->stream>>>(M);
+    TB_CHECK_LAUNCH(c);
+    for (int l = NL - 1; l >= 1; l--) {
+        size_t pf = (size_t)m->ptsx[l - 1] * m->ptsy[l - 1] * K;
+        if (m->semi[l - 1]) k_prolong_x<<<tb_blocks(pf, 256), 256, 0, c->stream>>>(M, l);
+        else k_prolong32<<<tb_blocks(pf, 256), 256, 0, c->stream>>>(M, l);
+        TB_CHECK_LAUNCH(c);
+        for (int s = 0; s < NU_POST; s++)
+            if ((r = sweep(c, M, l - 1))) return r;
+    }
+    return TB_OK;
+}
+
+}  // namespace
 
 int tb_mixed_setup(tb_ctx* c) {
-    (void)c;
-    tb_set_error("mixed-precision form not available in this build");
-    return TB_ERR_ARG;
+    tb_mixed_free(c);
+    const int K = c->g.K, ny = c->g.ny, msh = c->g.msh;
+    Mixed* m = new Mixed();
+    c->mixed = m;
+    // hierarchy: x-only coarsening while dx < max dy (if enabled), the
+    // reference's y-levels with x and y halved together, then x-only
+    // coarsening down to a level small enough for the direct solve
+    double dy_max = 0.0;
+    for (int j = 0; j + 1 < ny; j++) dy_max = std::max(dy_max, 1.0 / c->h_qdy[j]);
+    auto push = [&](int px, int py, int yl, double dx2) {
+        int l = m->NL++;
+        m->ptsx[l] = px; m->ptsy[l] = py; m->ylvl[l] = yl; m->dx2[l] = dx2; m->semi[l] = 0;
+    };
+    m->NL = 0;
+    push(c->g.nx, ny, 0, c->h_dx2[0]);
+    const int full_steps = msh - 1, fdiv = 1 << full_steps;
+    while (TB_MG_SEMI_FIRST && m->NL < MG_MAX - msh) {
+        int l = m->NL - 1, px = m->ptsx[l];
+        int pxn = (px + 1) / 2;
+        if (std::sqrt(m->dx2[l]) >= dy_max || (px - 1) % 2 || (pxn - 1) % fdiv || (pxn - 1) / fdiv + 1 < 10) break;
+        m->semi[l] = 1;
+        push(pxn, m->ptsy[l], 0, 4.0 * m->dx2[l]);
+    }
+    for (int yl = 1; yl <= full_steps; yl++) {
+        int l = m->NL - 1;
+        push((m->ptsx[l] + 1) / 2, c->g.ptsy[yl], yl, 4.0 * m->dx2[l]);
+    }
+    while (m->NL < MG_MAX) {
+        int l = m->NL - 1, px = m->ptsx[l], py = m->ptsy[l];
+        if ((long)(px - 2) * (py - 1) <= DIRECT_MAX || (px - 1) % 2 || (px + 1) / 2 < 10) break;
+        m->semi[l] = 1;
+        push((px + 1) / 2, py, m->ylvl[l], 4.0 * m->dx2[l]);
+    }
+    const int NL = m->NL, lc = NL - 1;
+    if (m->ptsx[lc] < 10) {
+        tb_set_error("mixed form needs at least 10 points in x on the coarsest level (got %d)", m->ptsx[lc]);
+        return TB_ERR_ARG;
+    }
+    m->N = (m->ptsx[lc] - 2) * (m->ptsy[lc] - 1);
+    if (m->N > DIRECT_LIMIT) {
+        tb_set_error("mixed form: coarsest level has %d unknowns per mode (limit %d); raise msh", m->N, DIRECT_LIMIT);
+        return TB_ERR_ARG;
+    }
+    size_t off = 0;
+    for (int l = 0; l < NL; l++) { m->off[l] = off; off += (size_t)m->ptsx[l] * m->ptsy[l]; m->S[l] = pick_S(m->ptsy[l]); }
+    m->elems = off;
+    size_t w = (size_t)K * m->elems;
+    for (float2** p : {&m->e, &m->r, &m->rr}) {
+        TB_CUDA(cudaMalloc(p, w * sizeof(float2)));
+        TB_CUDA(cudaMemset(*p, 0, w * sizeof(float2)));
+    }
+    // line-solve tables per (type, level, mode): band5 factors of the level's
+    // y-line matrix and chunk tables for this form's rows per lane, in FP32
+    const size_t bs = tb_poi_blk_size(ny);
+    std::vector<float> t32((size_t)2 * NL * K * bs, 0.f);
+    std::vector<double> a, blk(bs);
+    for (int type = 0; type < 2; type++)
+        for (int l = 0; l < NL; l++)
+            for (int k = 0; k < K; k++) {
+                int n = m->ptsy[l];
+                std::fill(blk.begin(), blk.end(), 0.0);
+                tb_poisson_band_matrix_dx(c, type, m->ylvl[l] + 1, k + 1, m->dx2[l], a);
+                tb_band5_factor(n, a, &blk[0], &blk[ny], &blk[2 * ny], &blk[3 * ny], &blk[4 * ny]);
+                tb_chunk_tables(n, ny, m->S[l], &blk[0], &blk[ny], &blk[2 * ny], &blk[3 * ny], &blk[4 * ny], &blk[5 * ny]);
+                float* D = &t32[(((size_t)type * NL + l) * K + k) * bs];
+                for (size_t q = 0; q < bs; q++) D[q] = (float)blk[q];
+            }
+    int r;
+    if ((r = upl(&m->tab, t32))) return r;
+    const double* blob = c->coefs.data();
+    std::vector<double> cf64((size_t)24 * msh);
+    for (int l = 0; l < msh; l++) {   // sp_poi(7,msh) cp_poi(8,msh) pp_poi(4,msh) lp_poi(5,msh) from blob[83]
+        for (int q = 0; q < 7; q++) cf64[24 * l + q] = blob[83 + 7 * l + q];
+        for (int q = 0; q < 8; q++) cf64[24 * l + 7 + q] = blob[83 + 7 * msh + 8 * l + q];
+        for (int q = 0; q < 4; q++) cf64[24 * l + 15 + q] = blob[83 + 15 * msh + 4 * l + q];
+        for (int q = 0; q < 5; q++) cf64[24 * l + 19 + q] = blob[83 + 19 * msh + 5 * l + q];
+    }
+    std::vector<float> cf(cf64.begin(), cf64.end());
+    if ((r = upl(&m->coef, cf))) return r;
+    std::vector<float> q2(c->h_qdy2.begin(), c->h_qdy2.end());
+    if ((r = upl(&m->qdy2, q2))) return r;
+    // exact inverse of the coarsest operator per mode (modes in parallel)
+    const int N = m->N;
+    std::vector<float> ainv((size_t)K * N * N);
+    std::vector<int> ok(K, 0);
+    auto work = [&](int k0, int k1) {
+        for (int k = k0; k < k1; k++) {
+            HostOp op;
+            const double* base = &cf64[24 * m->ylvl[lc]];
+            op.SP = base; op.CP = base + 7; op.PP = base + 15; op.LP = base + 19;
+            op.Q2 = &c->h_qdy2[(size_t)ny * m->ylvl[lc]];
+            op.den = 1.0 / (12.0 * m->dx2[lc] * c->cfg.fac_y);
+            op.ify = 1.0 / c->cfg.fac_y;
+            op.k2b2 = c->h_k2b2[k];
+            op.topc = std::sqrt((c->cfg.alpha * c->cfg.alpha - op.k2b2) / c->cfg.fac_y);
+            op.nxl = m->ptsx[lc]; op.n = m->ptsy[lc];
+            ok[k] = coarse_inverse(op, N, &ainv[(size_t)k * N * N]);
+        }
+    };
+    int nt = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)K);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++) th.emplace_back(work, K * t / nt, K * (t + 1) / nt);
+    for (auto& t : th) t.join();
+    for (int k = 0; k < K; k++)
+        if (!ok[k]) { tb_set_error("mixed form: coarsest operator of mode %d is singular", k); return TB_ERR_ARG; }
+    if ((r = upl(&m->ainv, ainv))) return r;
+    return TB_OK;
 }
-void tb_mixed_free(tb_ctx* c) { (void)c; }
+
+void tb_mixed_free(tb_ctx* c) {
+    Mixed* m = get(c);
+    if (!m) return;
+    for (void* p : {(void*)m->e, (void*)m->r, (void*)m->rr, (void*)m->tab, (void*)m->coef, (void*)m->qdy2, (void*)m->ainv})
+        if (p) cudaFree(p);
+    delete m;
+    c->mixed = nullptr;
+}
+
+// poi_uy (poisson_par.f:6-64), mixed form: at most max_vcycles FP64
+// corrections per solve; stats.vcycles[k] counts the corrections applied to
+// mode k.
 int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
-    (void)c; (void)dwzdx; (void)erro;
-    tb_set_error("mixed-precision form not available in this build");
-    return TB_ERR_ARG;
+    if (!c->mixed) { tb_set_error("mixed form not set up"); return TB_ERR_STATE; }
+    const int K = c->g.K, nx = c->g.nx, ny = c->g.ny, max_outer = c->cfg.max_vcycles;
+    MgDev M = make(c);
+    int r;
+    cudaEvent_t pall = nullptr;
+    if ((r = tb_prof_begin(c, PROF_POISSON, &pall))) return r;
+    if ((r = tb_poisson_begin(c, dwzdx))) return r;
+    std::vector<int> hs(2 * K);
+    dim3 tgrid(tb_blocks(nx, 32), tb_blocks(ny, 32), K), tblk(32, 8);
+    for (int it = 0; it <= max_outer; it++) {
+        if ((r = tb_poisson_fine_defect(c))) return r;
+        k_check_mixed<<<K, 256, 0, c->stream>>>(c->pdef, c->pstate, c->perr, nx, ny, erro, it, it == max_outer);
+        TB_CHECK_LAUNCH(c);
+        if (it == max_outer) break;
+        TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        TB_CUDA(cudaStreamSynchronize(c->stream));
+        bool any = false;
+        for (int k = 0; k < K; k++) any = any || hs[2 * k];
+        if (!any) break;
+        k_seed<<<tgrid, tblk, 0, c->stream>>>(M, c->pdef, nx, ny);
+        TB_CHECK_LAUNCH(c);
+        for (int v = 0; v < INNER_VCYCLES; v++)
+            if ((r = vcycle(c, M))) return r;
+        k_apply<<<tgrid, tblk, 0, c->stream>>>(M, c->pfc, c->g.lvl_elems, nx, ny);
+        TB_CHECK_LAUNCH(c);
+    }
+    if ((r = tb_poisson_end(c))) return r;
+    if ((r = tb_prof_end(c, PROF_POISSON, pall))) return r;
+    std::vector<double> he(K);
+    TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TB_CUDA(cudaMemcpyAsync(he.data(), c->perr, K * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    TB_CUDA(cudaStreamSynchronize(c->stream));
+    c->stats.noconv = 0;
+    int nonfinite = 0;
+    for (int k = 0; k < K && k < 256; k++) {
+        int vc = hs[2 * k + 1];
+        if (hs[2 * k]) c->stats.noconv++;
+        if (vc < 0) { nonfinite = 1; vc = -vc - 1; }
+        c->stats.vcycles[k] = vc;
+        c->stats.residual[k] = he[k];
+        c->stats.total_vcycles += vc;
+    }
+    c->stats.solves++;
+    if (nonfinite) { tb_set_error("poi_uy (mixed form): non-finite defect"); return TB_ERR_NONFINITE; }
+    return TB_OK;
 }

@@ -15,7 +15,7 @@
 #include <cstring>
 #include <algorithm>
 
-void tb_poisson_band_matrix(const tb_ctx* c, int type, int lvl, int k, std::vector<double>& a);
+
 
 namespace {
 
@@ -446,10 +446,12 @@ PoiDev make_dev(tb_ctx* c) {
     return P;
 }
 
-// Host: chunk tables of the line solve for one (type, level, mode).
-void chunk_tables(int n, int ny, const double* L1, const double* L2, const double* U1, const double* U2, const double* ID,
-                  double* out) {
-    int S = std::max(2, (n + 31) / 32);
+}  // namespace
+
+// Host: chunk tables of the line solve for one (type, level, mode), lane
+// chunks of S rows (lane t owns rows [tS, min(n, tS + S))).
+void tb_chunk_tables(int n, int ny, int S, const double* L1, const double* L2, const double* U1, const double* U2,
+                     const double* ID, double* out) {
     double *h1 = out, *h2 = out + ny, *k1 = out + 2 * ny, *k2 = out + 3 * ny;
     double* Pf = out + 4 * ny;
     double* Pb = Pf + 640;
@@ -504,39 +506,6 @@ void chunk_tables(int n, int ny, const double* L1, const double* L2, const doubl
     }
 }
 
-void band5_host(int n, std::vector<double>& a, double* L1, double* L2, double* U1, double* U2, double* ID) {
-    std::vector<double> al((size_t)n * 5, 0.0);
-    auto A = [&](int i, int c) -> double& { return a[(size_t)(i - 1) + (size_t)n * (c - 1)]; };
-    auto AL = [&](int i, int c) -> double& { return al[(size_t)(i - 1) + (size_t)n * (c - 1)]; };
-    const double TINY = (double)1.e-20f;
-    int m1 = 2, mm = 5, l = m1;
-    for (int i = 1; i <= m1; i++) {
-        for (int j = m1 + 2 - i; j <= mm; j++) A(i, j - l) = A(i, j);
-        l--;
-        for (int j = mm - l; j <= mm; j++) A(i, j) = 0.0;
-    }
-    l = m1;
-    for (int k = 1; k <= n; k++) {
-        double dum = A(k, 1);
-        if (l < n) l++;
-        if (dum == 0.0) A(k, 1) = TINY;
-        for (int i = k + 1; i <= l; i++) {
-            dum = A(i, 1) / A(k, 1);
-            AL(k, i - k) = dum;
-            for (int j = 2; j <= mm; j++) A(i, j - 1) = A(i, j) - dum * A(k, j);
-            A(i, mm) = 0.0;
-        }
-    }
-    for (int j = 1; j <= n; j++) {
-        L1[j - 1] = (j >= 2) ? AL(j - 1, 1) : 0.0;
-        L2[j - 1] = (j >= 3) ? AL(j - 2, 2) : 0.0;
-        U1[j - 1] = (j <= n - 1) ? A(j, 2) : 0.0;
-        U2[j - 1] = (j <= n - 2) ? A(j, 3) : 0.0;
-        ID[j - 1] = 1.0 / A(j, 1);
-    }
-}
-
-}  // namespace
 
 int tb_poisson_setup(tb_ctx* c) {
     int ny = c->g.ny, K = c->g.K, msh = c->g.msh;
@@ -548,8 +517,9 @@ int tb_poisson_setup(tb_ctx* c) {
                 tb_poisson_band_matrix(c, type, l + 1, k + 1, a);
                 int n = c->g.ptsy[l];
                 double* T = &all[(((size_t)type * msh + l) * K + k) * bs];
-                band5_host(n, a, T, T + ny, T + 2 * ny, T + 3 * ny, T + 4 * ny);
-                chunk_tables(n, ny, T, T + ny, T + 2 * ny, T + 3 * ny, T + 4 * ny, T + 5 * ny);
+                tb_band5_factor(n, a, T, T + ny, T + 2 * ny, T + 3 * ny, T + 4 * ny);
+                tb_chunk_tables(n, ny, std::max(2, (n + 31) / 32), T, T + ny, T + 2 * ny, T + 3 * ny, T + 4 * ny,
+                                T + 5 * ny);
             }
     if (c->pcarry) cudaFree(c->pcarry);
     TB_CUDA(cudaMalloc(&c->pcarry, all.size() * sizeof(double)));
@@ -653,5 +623,36 @@ int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro) {
     }
     c->stats.solves++;
     if (nonfinite) { tb_set_error("poi_uy: non-finite defect"); return TB_ERR_NONFINITE; }
+    return TB_OK;
+}
+
+// Pieces of poi_uy shared with the mixed form: the source and the start
+// state (fc = uy, every mode active), the FP64 fine-level defect
+// def = sc - L fc, and the write-back of fc into uy.
+int tb_poisson_begin(tb_ctx* c, const cplx* dwzdx) {
+    PoiDev P = make_dev(c);
+    double stf_pow = tb_powi(c->cfg.stf, c->g.ny - 3);
+    k_source<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(P, c->wx, dwzdx, c->uy, c->duexmdx, c->uyb, c->cfg.beta,
+                                                               c->cfg.dy, stf_pow, c->cfg.my_form);
+    TB_CHECK_LAUNCH(c);
+    k_activate<<<tb_blocks(c->g.K, 64), 64, 0, c->stream>>>(c->pstate, c->g.K);
+    TB_CHECK_LAUNCH(c);
+    return TB_OK;
+}
+
+int tb_poisson_fine_defect(tb_ctx* c) {
+    PoiDev P = make_dev(c);
+    size_t per = (size_t)(c->g.nx - 2) * (c->g.ny - 1) * c->g.K;
+    cudaEvent_t ps = nullptr;
+    if (tb_prof_begin(c, PROF_DEFECT, &ps)) return TB_ERR_CUDA;
+    k_defect<<<tb_blocks(per, 256), 256, 0, c->stream>>>(P, 0, -1.0);
+    TB_CHECK_LAUNCH(c);
+    return tb_prof_end(c, PROF_DEFECT, ps);
+}
+
+int tb_poisson_end(tb_ctx* c) {
+    PoiDev P = make_dev(c);
+    k_write_uy<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(P, c->uy);
+    TB_CHECK_LAUNCH(c);
     return TB_OK;
 }
