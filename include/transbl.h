@@ -182,8 +182,10 @@ long long tb_launch_count(tb_ctx* ctx);
 /* CUDA-event timing of kernel families on the context stream: enable = 1
    starts recording (and clears totals), 0 stops.  tb_profile_read returns the
    accumulated device milliseconds and launch count of one family:
-   0 line-SOR sweeps, 1 whole poi_uy, 2 nlterms, 3 x-line batches,
-   4 y-line batches, 5 RK stages, 6 x-penta solves, 7 Poisson defects. */
+   0 line-relaxation sweeps (SOR in the plain form, coloured sweeps in the
+   mixed form), 1 whole poi_uy, 2 nlterms, 3 x-line batches, 4 y-line
+   batches, 5 RK stages, 6 x-penta solves, 7 FP64 Poisson defects,
+   8 single finest-level line-relaxation launches of the mixed form. */
 int tb_profile(tb_ctx* ctx, int enable);
 int tb_profile_read(tb_ctx* ctx, int family, double* ms, long long* launches);
 

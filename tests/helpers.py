@@ -3,7 +3,8 @@ import numpy as np
 
 from trans_bl_gb300 import api, configs
 
-NAMES = ("ux", "uy", "uz", "wx", "wy", "wz")
+NAMES = configs.NAMES
+smooth_random = configs.smooth_random
 
 
 def small_case(**kw):
@@ -12,35 +13,8 @@ def small_case(**kw):
     return cfg, coefs, base
 
 
-def smooth_random(shape, rng, scale=1.0):
-    """Complex field with mode 0 real, smooth in x and y (sum of few waves)."""
-    K, ny, nx = shape
-    x = np.linspace(0, 1, nx)[None, :]
-    y = np.linspace(0, 1, ny)[:, None]
-    f = np.zeros(shape, dtype=np.complex128)
-    for k in range(K):
-        acc = np.zeros((ny, nx), dtype=np.complex128)
-        for _ in range(3):
-            a, b = rng.uniform(0.5, 4.0, 2)
-            p = rng.uniform(0, 2 * np.pi, 2)
-            c = rng.normal() + 1j * rng.normal()
-            acc += c * np.sin(a * np.pi * x + p[0]) * np.cos(b * np.pi * y + p[1])
-        f[k] = acc * scale / (1 + k)
-    f[0] = f[0].real
-    return f
-
-
 def perturbed_state(cfg, base, rng, amp=1e-3):
-    uxb, uyb, wzb = base
-    st = {}
-    for n in NAMES:
-        st[n] = smooth_random((cfg.kfour, cfg.ny, cfg.nx), rng, amp)
-    for n in ("ux", "uy", "uz"):   # no-slip wall row, as in every state of a run
-        st[n][:, 0, :] = 0.0
-    st["ux"][0] += uxb
-    st["uy"][0] += uyb
-    st["wz"][0] += wzb
-    return st
+    return configs.disturbed_state(cfg, base, rng, amp)
 
 
 def rel(a, b):

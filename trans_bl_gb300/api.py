@@ -254,7 +254,8 @@ class Context:
         self._c(self.lib.tb_stream(self.h, C.byref(p)), "tb_stream")
         return p.value
 
-    PROF = {"sor": 0, "poi_uy": 1, "nlterms": 2, "xlines": 3, "ylines": 4, "stage": 5, "penta": 6, "defect": 7}
+    PROF = {"sor": 0, "poi_uy": 1, "nlterms": 2, "xlines": 3, "ylines": 4, "stage": 5, "penta": 6, "defect": 7,
+            "relax0": 8}
 
     def profile(self, enable):
         self._c(self.lib.tb_profile(self.h, 1 if enable else 0), "tb_profile")

@@ -57,7 +57,15 @@ def config1(**kw):
 
 
 def config2(**kw):
-    """3D: nx=1025, ny=193, 32 modes (P=64), 2D TS + oblique pair, 4-level multigrid."""
+    """3D: nx=1025, ny=193, 32 modes (P=64), 2D TS + oblique pair, 4-level multigrid.
+
+    1024 steps per forcing period: with the 1.02 stretching to 40 delta* over
+    193 points the first wall cell is dy0 = 5.4e-5 L, and the explicit RK4
+    viscous term is stable only for nu dt lambda_max < 2.78 with lambda_max =
+    6.86 / dy0^2 (compact 6th-order second derivative at the grid scale).  At
+    256 steps per period nu dt lambda_max = 5.0 and the run diverges within
+    ten steps from the undisturbed base flow; at 1024 it is 1.26."""
+    kw.setdefault("steps_per_period", 1024)
     kw.setdefault("amp2d", 1e-4)
     kw.setdefault("amp3d", 1e-5)
     return blasius_ts_config(1025, 193, 32, 64, 4, **kw)
@@ -69,6 +77,42 @@ def small(nx=65, ny=33, kfour=4, kphys=8, msh=3, **kw):
     kw.setdefault("n_lambda", 4.0)
     kw.setdefault("strip", (1.0, 1.6))
     return blasius_ts_config(nx, ny, kfour, kphys, msh, **kw)
+
+
+NAMES = ("ux", "uy", "uz", "wx", "wy", "wz")
+
+
+def smooth_random(shape, rng, scale=1.0):
+    """Complex field with mode 0 real, smooth in x and y (sum of few waves)."""
+    K, ny, nx = shape
+    x = np.linspace(0, 1, nx)[None, :]
+    y = np.linspace(0, 1, ny)[:, None]
+    f = np.zeros(shape, dtype=np.complex128)
+    for k in range(K):
+        acc = np.zeros((ny, nx), dtype=np.complex128)
+        for _ in range(3):
+            a, b = rng.uniform(0.5, 4.0, 2)
+            p = rng.uniform(0, 2 * np.pi, 2)
+            c = rng.normal() + 1j * rng.normal()
+            acc += c * np.sin(a * np.pi * x + p[0]) * np.cos(b * np.pi * y + p[1])
+        f[k] = acc * scale / (1 + k)
+    f[0] = f[0].real
+    return f
+
+
+def disturbed_state(cfg, base, rng, amp=1e-3):
+    """Base flow plus a smooth seeded disturbance of relative size amp in
+    every field and mode; velocities keep the no-slip wall row."""
+    uxb, uyb, wzb = base
+    st = {}
+    for n in NAMES:
+        st[n] = smooth_random((cfg.kfour, cfg.ny, cfg.nx), rng, amp)
+    for n in ("ux", "uy", "uz"):
+        st[n][:, 0, :] = 0.0
+    st["ux"][0] += uxb
+    st["uy"][0] += uyb
+    st["wz"][0] += wzb
+    return st
 
 
 def setup_inputs(cfg):

@@ -115,7 +115,7 @@ struct tb_ctx {
 
 // Kernel families timed by tb_profile (index into prof_ms / prof_n).
 enum ProfId { PROF_SOR = 0, PROF_POISSON = 1, PROF_NLTERMS = 2, PROF_XLINES = 3, PROF_YLINES = 4,
-              PROF_STAGE = 5, PROF_PENTA = 6, PROF_DEFECT = 7, PROF_COUNT = 8 };
+              PROF_STAGE = 5, PROF_PENTA = 6, PROF_DEFECT = 7, PROF_RELAX0 = 8, PROF_COUNT = 9 };
 int tb_prof_begin(tb_ctx* c, int id, cudaEvent_t* start);
 int tb_prof_end(tb_ctx* c, int id, cudaEvent_t start);
 

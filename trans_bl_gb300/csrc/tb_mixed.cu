@@ -618,6 +618,9 @@ bool coarse_inverse(const HostOp& op, int N, float* out) {
 }
 
 int launch_relax(tb_ctx* c, const MgDev& M, int S, int l, int first, int step, int nlines) {
+    cudaEvent_t p0 = nullptr;
+    int r;
+    if (l == 0 && (r = tb_prof_begin(c, PROF_RELAX0, &p0))) return r;
     int nw = nlines * c->g.K;
     unsigned nb = tb_blocks((size_t)nw, RELAX_THREADS / 32);
     size_t smem = (size_t)(RELAX_THREADS / 32) * 2 * M.ptsy[l] * sizeof(float2);
@@ -635,7 +638,7 @@ int launch_relax(tb_ctx* c, const MgDev& M, int S, int l, int first, int step, i
         default: k_relax<16><<<nb, RELAX_THREADS, smem, st>>>(M, l, first, step, nlines); break;
     }
     TB_CHECK_LAUNCH(c);
-    return TB_OK;
+    return l == 0 ? tb_prof_end(c, PROF_RELAX0, p0) : TB_OK;
 }
 
 // One relaxation sweep at level l: border lines, then centre colours 0, 1, 2.
