@@ -133,7 +133,9 @@ int tb_destroy(tb_ctx* c) {
     void* ptrs[] = {c->ux, c->uy, c->uz, c->wx, c->wy, c->wz, c->wx1, c->wy1, c->wz1, c->dv1x, c->dv1y, c->dv1z, c->dv2x,
                     c->dv2y, c->dv2z, c->d2uydx2, c->lapv, c->uxb, c->uyb, c->wzb, c->duexmdx, c->bdfc, c->fcx, c->fcllx,
                     c->gibbs, c->delta_no, c->k2b2, c->tx1.a, c->tx1.g, c->tx1.ib, c->tx2.a, c->tx2.g, c->tx2.ib,
-                    c->tfil.a, c->tfil.g, c->tfil.ib, c->ty1.a, c->ty1.g, c->ty1.ib, c->tyfv.a, c->tyfv.g, c->tyfv.ib,
+                    c->tfil.a, c->tfil.g, c->tfil.ib,
+                    c->tx1.hf, c->tx1.hb, c->tx1.pf, c->tx1.pb, c->tx2.hf, c->tx2.hb, c->tx2.pf, c->tx2.pb,
+                    c->tfil.hf, c->tfil.hb, c->tfil.pf, c->tfil.pb, c->ty1.a, c->ty1.g, c->ty1.ib, c->tyfv.a, c->tyfv.g, c->tyfv.ib,
                     c->ty2.a, c->ty2.g, c->ty2.ib, c->ry1.w, c->ry1.off, c->ry1.cnt, c->ryfv.w, c->ryfv.off, c->ryfv.cnt,
                     c->ry2.w, c->ry2.off, c->ry2.cnt, c->px.lu, c->pfc, c->psc, c->pfct, c->pdef, c->pcarry,
                     c->pstate, c->perr, c->pqdy2, c->pcoef};

@@ -118,13 +118,51 @@ int upload(T** dst, const std::vector<T>& src) {
     return TB_OK;
 }
 
-int upload_tri(TriLHS& t, const std::vector<double>& a, const std::vector<double>& b, const std::vector<double>& c) {
+// Chunk tables of a Thomas sweep split over 32 lanes of S rows (TriLHS).
+void chunk_tri(const std::vector<double>& a, const std::vector<double>& g, const std::vector<double>& ib, int S,
+               std::vector<double>& hf, std::vector<double>& hb, std::vector<double>& pf, std::vector<double>& pb) {
+    int n = (int)a.size();
+    hf.assign(n, 0.0); hb.assign(n, 0.0); pf.assign(160, 0.0); pb.assign(160, 0.0);
+    double Af[32], Ab[32];
+    for (int t = 0; t < 32; t++) {
+        int r0 = t * S, r1 = std::min(n, r0 + S);
+        double h = 1.0;
+        for (int i = r0; i < r1; i++) { h *= -a[i] * ib[i]; hf[i] = h; }
+        Af[t] = (r1 > r0) ? hf[r1 - 1] : 1.0;
+        h = 1.0;
+        for (int i = r1 - 1; i >= r0; i--) { h = (r1 < n) ? h * -g[i + 1] : 0.0; hb[i] = h; }
+        Ab[t] = (r1 > r0) ? hb[r0] : 1.0;
+    }
+    for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
+        double nf[32], nb[32];
+        for (int t = 0; t < 32; t++) {
+            pf[d * 32 + t] = Af[t];
+            pb[d * 32 + t] = Ab[t];
+            nf[t] = (t >= off) ? Af[t] * Af[t - off] : Af[t];
+            nb[t] = (t + off < 32) ? Ab[t] * Ab[t + off] : Ab[t];
+        }
+        std::copy(nf, nf + 32, Af);
+        std::copy(nb, nb + 32, Ab);
+    }
+}
+
+int upload_tri(TriLHS& t, const std::vector<double>& a, const std::vector<double>& b, const std::vector<double>& c,
+               bool chunked = false) {
     std::vector<double> g, ib;
     thomas_factors(a, b, c, g, ib);
     int r;
     if ((r = upload(&t.a, a))) return r;
     if ((r = upload(&t.g, g))) return r;
-    return upload(&t.ib, ib);
+    if ((r = upload(&t.ib, ib))) return r;
+    if (!chunked) return TB_OK;
+    int n = (int)a.size();
+    t.S = (n + 31) / 32;
+    std::vector<double> hf, hb, pf, pb;
+    chunk_tri(a, g, ib, t.S, hf, hb, pf, pb);
+    if ((r = upload(&t.hf, hf))) return r;
+    if ((r = upload(&t.hb, hb))) return r;
+    if ((r = upload(&t.pf, pf))) return r;
+    return upload(&t.pb, pb);
 }
 
 // lhs5 (loop_par.f:258-299) + ludecomp (penta_par.f:6-50), 1-based (n,5).
@@ -292,14 +330,14 @@ int tb_host_build_tables(tb_ctx* c) {
         a[0] = 0; b[0] = 1; cc[0] = 0; a[1] = 1; b[1] = 6; cc[1] = 2;
         for (int i = 2; i < nx - 2; i++) { a[i] = 1; b[i] = 3; cc[i] = 1; }
         a[nx - 2] = 2; b[nx - 2] = 6; cc[nx - 2] = 1; a[nx - 1] = 4; b[nx - 1] = 1; cc[nx - 1] = 0;
-        if ((r = upload_tri(c->tx1, a, b, cc))) return r;
+        if ((r = upload_tri(c->tx1, a, b, cc, true))) return r;
         a[0] = 0; b[0] = 13; cc[0] = 137; a[1] = 1; b[1] = 12; cc[1] = 3;
         for (int i = 2; i < nx - 2; i++) { a[i] = 2; b[i] = 11; cc[i] = 2; }
         a[nx - 2] = 3; b[nx - 2] = 12; cc[nx - 2] = 1; a[nx - 1] = 137; b[nx - 1] = 13; cc[nx - 1] = 0;
-        if ((r = upload_tri(c->tx2, a, b, cc))) return r;
+        if ((r = upload_tri(c->tx2, a, b, cc, true))) return r;
         std::fill(a.begin(), a.end(), 0.0); std::fill(b.begin(), b.end(), 1.0); std::fill(cc.begin(), cc.end(), 0.0);
         for (int i = 3; i < nx - 3; i++) { a[i] = cf.alphaf; cc[i] = cf.alphaf; }
-        if ((r = upload_tri(c->tfil, a, b, cc))) return r;
+        if ((r = upload_tri(c->tfil, a, b, cc, true))) return r;
     }
     // y compact LHS (coefy/coefy_fv/coeffy derivs_par.f:1040-1142) and RHS row weights
     {

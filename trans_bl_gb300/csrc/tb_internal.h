@@ -39,6 +39,15 @@ struct TriLHS {
     double* a;   // (n)
     double* g;   // (n) gam
     double* ib;  // (n) 1/bet
+    // Chunked form for one warp per line (x-lines): lane t owns rows
+    // [tS, min(n, tS + S)).  hf_i = d u_i / d u_{tS-1} of the forward sweep,
+    // hb_i = d x_i / d x_{tS+S} of the backward sweep, and the Kogge-Stone
+    // step factors pf[d][t], pb[d][t] of the chunk-end (start) responses.
+    double* hf = nullptr;   // (n)
+    double* hb = nullptr;   // (n)
+    double* pf = nullptr;   // (5, 32)
+    double* pb = nullptr;   // (5, 32)
+    int S = 0;
 };
 // Row weights of the stretched-y compact RHS: row j (0-based) is
 // sum_m w[7*j+m] * f[j + off[j] + m], m < cnt[j].
@@ -162,7 +171,7 @@ int tb_ts_pert_k(tb_ctx* c, int t, double tempt);
 int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro);
 int tb_poisson_setup(tb_ctx* c);
 int tb_poisson_begin(tb_ctx* c, const cplx* dwzdx);
-int tb_poisson_fine_defect(tb_ctx* c);
+int tb_poisson_defect_f32(tb_ctx* c, float2* r32, float2* e32, size_t elems32, unsigned long long* maxsq);
 int tb_poisson_end(tb_ctx* c);
 void tb_chunk_tables(int n, int ny, int S, const double* L1, const double* L2, const double* U1, const double* U2,
                      const double* ID, double* out);

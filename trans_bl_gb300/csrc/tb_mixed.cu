@@ -66,6 +66,7 @@ struct Mixed {
     float* coef = nullptr;    // sp(7) cp(8) pp(4) lp(5) per reference level
     float* qdy2 = nullptr;    // (ny, msh)
     float* ainv = nullptr;    // (K, N, N) inverse of the coarsest operator per mode
+    unsigned long long* maxsq = nullptr;   // (K) max |defect|^2 as double bits
     int NL = 0, N = 0;
     int ptsx[MG_MAX], ptsy[MG_MAX], ylvl[MG_MAX], semi[MG_MAX], S[MG_MAX];
     double dx2[MG_MAX];
@@ -411,33 +412,6 @@ __global__ void k_direct(MgDev M) {
     if (lane == 0) M.e[(size_t)k * M.elems + M.off[l] + (size_t)n * (1 + p / m) + 1 + p % m] = f2(ax, ay);
 }
 
-// FP64 defect (x-contiguous) -> FP32 right-hand side r(0) (line-contiguous)
-// through a 32x32 shared-memory tile; e(0) = 0.
-__global__ void k_seed(MgDev M, const cplx* def, int nx, int ny) {
-    __shared__ float2 tile[32][33];
-    const int k = blockIdx.z;
-    if (!M.state[2 * k]) return;   // uniform over the block
-    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
-    for (int r = threadIdx.y; r < 32; r += 8) {
-        int i = i0 + threadIdx.x, j = j0 + r;
-        float2 v = f2(0.f, 0.f);
-        if (i >= 1 && i <= nx - 2 && j >= 1 && j < ny) {
-            cplx d = def[(size_t)k * nx * ny + (size_t)i + (size_t)nx * j];
-            v = f2((float)d.x, (float)d.y);
-        }
-        tile[r][threadIdx.x] = v;
-    }
-    __syncthreads();
-    for (int r = threadIdx.y; r < 32; r += 8) {
-        int i = i0 + r, j = j0 + threadIdx.x;
-        if (i < nx && j < ny) {
-            size_t o = (size_t)k * M.elems + M.off[0] + (size_t)ny * i + j;
-            M.r[o] = tile[threadIdx.x][r];
-            M.e[o] = f2(0.f, 0.f);
-        }
-    }
-}
-
 // u += e on the interior of the FP64 fine level (fc layout: x-contiguous).
 __global__ void k_apply(MgDev M, cplx* fc, size_t elems64, int nx, int ny) {
     __shared__ float2 tile[32][33];
@@ -462,37 +436,20 @@ __global__ void k_apply(MgDev M, cplx* fc, size_t elems64, int nx, int ny) {
 }
 
 // Per-mode test of the FP64 defect (max |d| over the interior, as
-// get_max_value/verifica_poi): converged modes leave the active set with
-// the number of corrections applied; a non-finite defect stops the mode
-// with -1 - corrections.
-__global__ void k_check_mixed(const cplx* def, int* state, double* err, int nx, int ny, double tol, int it, int last) {
-    int k = blockIdx.x;
-    if (!state[2 * k]) return;
-    const cplx* D = def + (size_t)k * nx * ny;
-    double m = 0.0;
-    int bad = 0;
-    for (int q = threadIdx.x; q < (nx - 2) * (ny - 1); q += blockDim.x) {
-        int i = 1 + q % (nx - 2), j = 1 + q / (nx - 2);
-        cplx v = D[(size_t)i + (size_t)nx * j];
-        double a = hypot(v.x, v.y);
-        if (!(a == a) || isinf(a)) bad = 1;
-        m = fmax(m, a);
-    }
-    __shared__ double red[256];
-    __shared__ int sbad;
-    if (threadIdx.x == 0) sbad = 0;
-    __syncthreads();
-    if (bad) sbad = 1;
-    red[threadIdx.x] = m;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        err[k] = sbad ? __longlong_as_double(0x7ff8000000000000LL) : red[0];
-        if (sbad) { state[2 * k] = 0; state[2 * k + 1] = -1 - it; }
-        else if (red[0] < tol) { state[2 * k] = 0; state[2 * k + 1] = it; }
+// get_max_value/verifica_poi, from the max |d|^2 the defect kernel folded
+// into maxsq): converged modes leave the active set with the number of
+// corrections applied; a non-finite defect stops the mode with
+// -1 - corrections.  maxsq is cleared for the next defect.
+__global__ void k_check_sq(unsigned long long* maxsq, int* state, double* err, int K, double tol, int it, int last) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K || !state[2 * k]) return;
+    double m2 = __longlong_as_double((long long)maxsq[k]);
+    maxsq[k] = 0ull;
+    double e = sqrt(m2);
+    if (!(e <= 1.7e308)) { err[k] = __longlong_as_double(0x7ff8000000000000LL); state[2 * k] = 0; state[2 * k + 1] = -1 - it; }
+    else {
+        err[k] = e;
+        if (e < tol) { state[2 * k] = 0; state[2 * k + 1] = it; }
         else if (last) state[2 * k + 1] = it;   // stays active: not converged
     }
 }
@@ -739,6 +696,8 @@ int tb_mixed_setup(tb_ctx* c) {
         TB_CUDA(cudaMalloc(p, w * sizeof(float2)));
         TB_CUDA(cudaMemset(*p, 0, w * sizeof(float2)));
     }
+    TB_CUDA(cudaMalloc(&m->maxsq, K * sizeof(unsigned long long)));
+    TB_CUDA(cudaMemset(m->maxsq, 0, K * sizeof(unsigned long long)));
     // line-solve tables per (type, level, mode): band5 factors of the level's
     // y-line matrix and chunk tables for this form's rows per lane, in FP32
     const size_t bs = tb_poi_blk_size(ny);
@@ -800,7 +759,8 @@ int tb_mixed_setup(tb_ctx* c) {
 void tb_mixed_free(tb_ctx* c) {
     Mixed* m = get(c);
     if (!m) return;
-    for (void* p : {(void*)m->e, (void*)m->r, (void*)m->rr, (void*)m->tab, (void*)m->coef, (void*)m->qdy2, (void*)m->ainv})
+    for (void* p : {(void*)m->e, (void*)m->r, (void*)m->rr, (void*)m->tab, (void*)m->coef, (void*)m->qdy2, (void*)m->ainv,
+                    (void*)m->maxsq})
         if (p) cudaFree(p);
     delete m;
     c->mixed = nullptr;
@@ -820,8 +780,9 @@ int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
     std::vector<int> hs(2 * K);
     dim3 tgrid(tb_blocks(nx, 32), tb_blocks(ny, 32), K), tblk(32, 8);
     for (int it = 0; it <= max_outer; it++) {
-        if ((r = tb_poisson_fine_defect(c))) return r;
-        k_check_mixed<<<K, 256, 0, c->stream>>>(c->pdef, c->pstate, c->perr, nx, ny, erro, it, it == max_outer);
+        Mixed* m = get(c);
+        if ((r = tb_poisson_defect_f32(c, m->r, m->e, m->elems, m->maxsq))) return r;
+        k_check_sq<<<tb_blocks(K, 64), 64, 0, c->stream>>>(m->maxsq, c->pstate, c->perr, K, erro, it, it == max_outer);
         TB_CHECK_LAUNCH(c);
         if (it == max_outer) break;
         TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -829,8 +790,6 @@ int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
         bool any = false;
         for (int k = 0; k < K; k++) any = any || hs[2 * k];
         if (!any) break;
-        k_seed<<<tgrid, tblk, 0, c->stream>>>(M, c->pdef, nx, ny);
-        TB_CHECK_LAUNCH(c);
         for (int v = 0; v < INNER_VCYCLES; v++)
             if ((r = vcycle(c, M))) return r;
         k_apply<<<tgrid, tblk, 0, c->stream>>>(M, c->pfc, c->g.lvl_elems, nx, ny);

@@ -42,7 +42,8 @@ struct PoiDev {
     int ptsx[TB_MAX_MSH], ptsy[TB_MAX_MSH];
     size_t off[TB_MAX_MSH], elems, dstride;
     double dx2[TB_MAX_MSH];
-    double fac_y, alpha;
+    double den[TB_MAX_MSH];       // 1 / (12 dx2 fac_y)
+    double fac_y, alpha, ify;
 };
 
 __device__ __forceinline__ cplx& AT(cplx* base, const PoiDev& P, int k, int l, int i, int j) {
@@ -236,23 +237,14 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor(PoiDev P, int l, int itera,
 }
 
 // ---------------------------------------------------------------------------
-// defect (poisson_par.f:543-793): def = sc + si * (L fc) at level l;
-// si > 0 also stores it into sc(l) (coarse right-hand side).
-__global__ void k_defect(PoiDev P, int l, double si) {
+// The level-l operator of defect (poisson_par.f:543-793) applied to fc at the
+// interior point (i, j) of mode k: L fc = den*Dxx + q2*Dyy + k2b2*ify*M - top.
+__device__ __forceinline__ cplx poi_Lu(const PoiDev& P, int l, int k, int i, int j) {
     const int nxl = P.ptsx[l], n = P.ptsy[l];
-    size_t per = (size_t)(nxl - 2) * (n - 1);
-    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (q >= per * P.K) return;
-    int k = (int)(q / per);
-    if (!P.state[2 * k]) return;
-    size_t rq = q % per;
-    int i = 1 + (int)(rq % (nxl - 2));
-    int j = 1 + (int)(rq / (nxl - 2));
     const double* cf = P.coef + 24 * l;
     const double *SPc = cf, *CPc = cf + 7, *PPc = cf + 15, *LPc = cf + 19;
     double k2b2 = P.k2b2[k];
-    double alpha2 = sqrt((P.alpha * P.alpha - k2b2) / P.fac_y);
-    double den = 1.0 / (12.0 * P.dx2[l] * P.fac_y), ify = 1.0 / P.fac_y;
+    double den = P.den[l], ify = P.ify;
     const cplx* F = P.fc + (size_t)k * P.elems + P.off[l];
     auto f = [&](int ii, int jj) -> cplx { return F[(size_t)ii + (size_t)nxl * jj]; };
     auto bx = [&](int jj) -> cplx {
@@ -296,15 +288,81 @@ __global__ void k_defect(PoiDev P, int l, double si) {
         cc = make_double2(LPc[2] * f0.x + LPc[3] * fm1.x + LPc[4] * fm2.x, LPc[2] * f0.y + LPc[3] * fm1.y + LPc[4] * fm2.y);
         d = make_double2(k2b2 * f0.x, k2b2 * f0.y);
         q2 = P.qdy2[(j - 2) + (size_t)P.ny * l];
+        double alpha2 = sqrt((P.alpha * P.alpha - k2b2) / P.fac_y);
         top = LPc[1] * alpha2 * sqrt(q2);
     }
     cplx fij = f(i, j);
+    return make_double2(b.x * den + cc.x * q2 + d.x * ify - top * fij.x, b.y * den + cc.y * q2 + d.y * ify - top * fij.y);
+}
+
+// defect (poisson_par.f:543-793): def = sc + si * (L fc) at level l;
+// si > 0 also stores it into sc(l) (coarse right-hand side).
+__global__ void k_defect(PoiDev P, int l, double si) {
+    const int nxl = P.ptsx[l], n = P.ptsy[l];
+    size_t per = (size_t)(nxl - 2) * (n - 1);
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * P.K) return;
+    int k = (int)(q / per);
+    if (!P.state[2 * k]) return;
+    size_t rq = q % per;
+    int i = 1 + (int)(rq % (nxl - 2));
+    int j = 1 + (int)(rq / (nxl - 2));
+    cplx Lu = poi_Lu(P, l, k, i, j);
     const cplx* SC = P.sc + (size_t)k * P.elems + P.off[l];
     cplx s = SC[(size_t)i + (size_t)nxl * j];
-    cplx v = make_double2(s.x + si * (b.x * den + cc.x * q2 + d.x * ify - top * fij.x),
-                          s.y + si * (b.y * den + cc.y * q2 + d.y * ify - top * fij.y));
+    cplx v = make_double2(s.x + si * Lu.x, s.y + si * Lu.y);
     P.def[(size_t)k * P.dstride + (size_t)i + (size_t)nxl * j] = v;
     if (si > 0) AT(P.sc, P, k, l, i, j) = v;
+}
+
+// Fine-level FP64 defect d = sc - L fc for the mixed form: stored as FP32 in
+// the line-contiguous right-hand side r32 of the correction equation (element
+// (i, j) of mode k at k*elems32 + i*ny + j, through a 32x32 shared tile), the
+// correction e32 zeroed at the same points, and max |d|^2 of each mode
+// folded into maxsq[k] (bit pattern of a non-negative double; a non-finite
+// defect records +inf).
+__global__ void k_defect_f32(PoiDev P, float2* r32, float2* e32, size_t elems32, unsigned long long* maxsq) {
+    __shared__ float2 tile[32][33];
+    __shared__ double wmax[8];
+    const int k = blockIdx.z;
+    if (!P.state[2 * k]) return;   // uniform over the block
+    const int nx = P.nx, ny = P.ny;
+    const int i0 = 1 + blockIdx.x * 32, j0 = 1 + blockIdx.y * 32;
+    double m = 0.0;
+    bool bad = false;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        int i = i0 + threadIdx.x, j = j0 + r;
+        float2 v32 = make_float2(0.f, 0.f);
+        if (i <= nx - 2 && j <= ny - 1) {
+            cplx s = P.sc[(size_t)k * P.elems + (size_t)i + (size_t)nx * j];
+            cplx Lu = poi_Lu(P, 0, k, i, j);
+            cplx v = make_double2(s.x - Lu.x, s.y - Lu.y);
+            double a = v.x * v.x + v.y * v.y;
+            if (!(a <= 1.7e308)) bad = true;
+            else m = fmax(m, a);
+            v32 = make_float2((float)v.x, (float)v.y);
+        }
+        tile[r][threadIdx.x] = v32;
+    }
+    if (bad) m = __longlong_as_double(0x7ff0000000000000LL);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const int w = (threadIdx.y * 32 + threadIdx.x) >> 5;
+    if ((threadIdx.x & 31) == 0) wmax[w] = m;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        double b = wmax[0];
+        for (int q = 1; q < 8; q++) b = fmax(b, wmax[q]);
+        atomicMax(&maxsq[k], (unsigned long long)__double_as_longlong(b));
+    }
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        int i = i0 + r, j = j0 + threadIdx.x;
+        if (i <= nx - 2 && j <= ny - 1) {
+            size_t o = (size_t)k * elems32 + (size_t)ny * i + j;
+            r32[o] = tile[threadIdx.x][r];
+            e32[o] = make_float2(0.f, 0.f);
+        }
+    }
 }
 
 // get_max_value + verifica_poi (poisson_par.f:67-108, 945-963): per mode.
@@ -440,7 +498,9 @@ PoiDev make_dev(tb_ctx* c) {
     P.nx = c->g.nx; P.ny = c->g.ny; P.K = c->g.K; P.msh = c->g.msh;
     for (int l = 0; l < c->g.msh; l++) {
         P.ptsx[l] = c->g.ptsx[l]; P.ptsy[l] = c->g.ptsy[l]; P.off[l] = c->g.lvl_off[l]; P.dx2[l] = c->h_dx2[l];
+        P.den[l] = 1.0 / (12.0 * c->h_dx2[l] * c->cfg.fac_y);
     }
+    P.ify = 1.0 / c->cfg.fac_y;
     P.elems = c->g.lvl_elems; P.dstride = (size_t)c->g.nx * c->g.ny;
     P.fac_y = c->cfg.fac_y; P.alpha = c->cfg.alpha;
     return P;
@@ -627,8 +687,7 @@ int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro) {
 }
 
 // Pieces of poi_uy shared with the mixed form: the source and the start
-// state (fc = uy, every mode active), the FP64 fine-level defect
-// def = sc - L fc, and the write-back of fc into uy.
+// state (fc = uy, every mode active) and the write-back of fc into uy.
 int tb_poisson_begin(tb_ctx* c, const cplx* dwzdx) {
     PoiDev P = make_dev(c);
     double stf_pow = tb_powi(c->cfg.stf, c->g.ny - 3);
@@ -640,19 +699,19 @@ int tb_poisson_begin(tb_ctx* c, const cplx* dwzdx) {
     return TB_OK;
 }
 
-int tb_poisson_fine_defect(tb_ctx* c) {
-    PoiDev P = make_dev(c);
-    size_t per = (size_t)(c->g.nx - 2) * (c->g.ny - 1) * c->g.K;
-    cudaEvent_t ps = nullptr;
-    if (tb_prof_begin(c, PROF_DEFECT, &ps)) return TB_ERR_CUDA;
-    k_defect<<<tb_blocks(per, 256), 256, 0, c->stream>>>(P, 0, -1.0);
-    TB_CHECK_LAUNCH(c);
-    return tb_prof_end(c, PROF_DEFECT, ps);
-}
-
 int tb_poisson_end(tb_ctx* c) {
     PoiDev P = make_dev(c);
     k_write_uy<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(P, c->uy);
     TB_CHECK_LAUNCH(c);
     return TB_OK;
+}
+
+int tb_poisson_defect_f32(tb_ctx* c, float2* r32, float2* e32, size_t elems32, unsigned long long* maxsq) {
+    PoiDev P = make_dev(c);
+    dim3 grid(tb_blocks(c->g.nx - 2, 32), tb_blocks(c->g.ny - 1, 32), c->g.K), blk(32, 8);
+    cudaEvent_t ps = nullptr;
+    if (tb_prof_begin(c, PROF_DEFECT, &ps)) return TB_ERR_CUDA;
+    k_defect_f32<<<grid, blk, 0, c->stream>>>(P, r32, e32, elems32, maxsq);
+    TB_CHECK_LAUNCH(c);
+    return tb_prof_end(c, PROF_DEFECT, ps);
 }
