@@ -417,6 +417,8 @@ int tb_host_build_tables(tb_ctx* c) {
             for (int m = 0; m < 5; m++) pc[24 * l + 19 + m] = co.lp_poi[5 * l + m];
         }
         if ((r = upload(&c->pcoef, pc))) return r;
+        const double* wat = c->coefs.data() + 100 + 24 * msh - 17;
+        if ((r = upload(&c->wcoef, std::vector<double>(wat, wat + 17)))) return r;
     }
     // var_ts (main_par.f:1688-1736)
     {

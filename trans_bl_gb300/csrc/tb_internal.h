@@ -107,6 +107,7 @@ struct tb_ctx {
     double* perr = nullptr;      // per mode max|defect|
     double* pqdy2 = nullptr;     // v_qdy2 on device (ny*msh)
     double* pcoef = nullptr;     // Poisson coefficients sp/cp/pp/lp per level (24*msh)
+    double* wcoef = nullptr;     // wall coefficients w_at_w_coef(9), dwydy_coef(8)
     // statistics
     tb_poisson_stats stats;
     // host staging for the mirrors

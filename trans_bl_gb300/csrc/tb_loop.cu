@@ -1,6 +1,7 @@
 // tb_loop.cu -- the stage driver (drv_fi/drv_les, RK4 update, wall forcing)
 // and the velocity recovery of loop() except the v-Poisson solve.
 #include "tb_internal.h"
+#include "tb_warp.cuh"
 #include <cmath>
 #include <cstring>
 
@@ -120,51 +121,131 @@ __global__ void k_copy_inner(cplx* dst, const cplx* src, int nx, int ny, int K) 
     dst[q] = src[q];
 }
 
-// poi_ux, fundamental mode (loop_par.f:452-499): ux from continuity by the
-// 4th-order implicit x integration, one thread per row j = 2..jmax-1.
-__global__ void k_ux_mode0(cplx* ux, const cplx* duydy, int nx, int ny, double dx) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    if (j > ny - 2) return;
-    cplx* U = ux + (size_t)nx * j;
-    const cplx* D = duydy + (size_t)nx * j;
+// ---------------------------------------------------------------------------
+// x-direction recurrences, one warp per line (tb_warp.cuh).  Shared memory
+// per warp: two line buffers of 32 x Sp complex (inputs E, rows V).
+
+// The 4th-order implicit x integration of poi_ux mode 0 (loop_par.f:452-499)
+// and of wz_wall (loop_par.f:361-425): w_0 given,
+//   w_1     = (sg dx (251 r0 + 646 r1 - 264 r2 + 106 r3 - 19 r4) + 720 w_0) / 720
+//   w_i     = (sg dx (281 r_{i-2} + 2056 r_{i-1} + 1176 r_i - 104 r_{i+1} + 11 r_{i+2}) / 90
+//              + 11 w_{i-2} + 16 w_{i-1}) / 27                       2 <= i <= n-3
+//   w_{n-2} = (sg dx (10 r_{n-4} + 57 r_{n-3} + 24 r_{n-2} - r_{n-1}) + 33 w_{n-4} + 24 w_{n-3}) / 57
+//   w_{n-1} = (sg dx (251 r_{n-1} + 646 r_{n-2} - 264 r_{n-3} + 106 r_{n-4} - 19 r_{n-5}) + 720 w_{n-2}) / 720
+// with r in E (lane chunks), w_0 = w0; the result (rows 1..n-1) goes to out.
+__device__ void xint_line(const cplx* E, cplx* V, const WarpLine& L, int lane, cplx w0, double sgdx, cplx* out) {
+    const int n = L.n, r0 = lane * L.S, r1 = min(n, r0 + L.S);
     const double i720 = 1.0 / 720.0, i27 = 1.0 / 27.0, i90 = 1.0 / 90.0, i57 = 1.0 / 57.0;
-    auto rr = [&](double a0, cplx d0, double a1, cplx d1, double a2, cplx d2, double a3, cplx d3, double a4, cplx d4) {
-        return make_double2(a0 * d0.x + a1 * d1.x + a2 * d2.x + a3 * d3.x + a4 * d4.x,
-                            a0 * d0.y + a1 * d1.y + a2 * d2.y + a3 * d3.y + a4 * d4.y);
+    auto e = [&](int i) { return E[L.slot(i)]; };
+    cplx* Vl = V + lane * L.Sp;
+    for (int i = r0; i < r1; i++) {
+        cplx v;
+        if (i == 0) v = w0;
+        else if (i == 1) {
+            cplx a = e(0), b = e(1), c = e(2), d = e(3), f = e(4);
+            v = make_double2(sgdx * (251.0 * a.x + 646.0 * b.x - 264.0 * c.x + 106.0 * d.x - 19.0 * f.x) * i720,
+                             sgdx * (251.0 * a.y + 646.0 * b.y - 264.0 * c.y + 106.0 * d.y - 19.0 * f.y) * i720);
+        } else if (i <= n - 3) {
+            cplx a = e(i - 2), b = e(i - 1), c = e(i), d = e(i + 1), f = e(i + 2);
+            v = make_double2(sgdx * (281.0 * a.x + 2056.0 * b.x + 1176.0 * c.x - 104.0 * d.x + 11.0 * f.x) * i90 * i27,
+                             sgdx * (281.0 * a.y + 2056.0 * b.y + 1176.0 * c.y - 104.0 * d.y + 11.0 * f.y) * i90 * i27);
+        } else if (i == n - 2) {
+            cplx a = e(i - 2), b = e(i - 1), c = e(i), d = e(i + 1);
+            v = make_double2(sgdx * (10.0 * a.x + 57.0 * b.x + 24.0 * c.x - d.x) * i57,
+                             sgdx * (10.0 * a.y + 57.0 * b.y + 24.0 * c.y - d.y) * i57);
+        } else {
+            cplx a = e(i), b = e(i - 1), c = e(i - 2), d = e(i - 3), f = e(i - 4);
+            v = make_double2(sgdx * (251.0 * a.x + 646.0 * b.x - 264.0 * c.x + 106.0 * d.x - 19.0 * f.x) * i720,
+                             sgdx * (251.0 * a.y + 646.0 * b.y - 264.0 * c.y + 106.0 * d.y - 19.0 * f.y) * i720);
+        }
+        Vl[i - r0] = v;
+    }
+    auto ca_ = [=](int i) -> double {
+        if (i == 0) return 0.0;
+        if (i == 1 || i == n - 1) return -720.0 * i720;
+        if (i == n - 2) return -24.0 * i57;
+        return -16.0 * i27;
     };
-    cplx u0 = U[0];
-    cplx s = rr(251.0, D[0], 646.0, D[1], -264.0, D[2], 106.0, D[3], -19.0, D[4]);
-    cplx u1 = make_double2((-dx * s.x + 720.0 * u0.x) * i720, (-dx * s.y + 720.0 * u0.y) * i720);
-    U[1] = u1;
-    cplx um2 = u0, um1 = u1;
-    cplx d0 = D[0], d1 = D[1], d2 = D[2], d3 = D[3];
-    for (int i = 2; i <= nx - 3; i++) {
-        cplx d4 = D[i + 2];
-        cplx t = rr(281.0, d0, 2056.0, d1, 1176.0, d2, -104.0, d3, 11.0, d4);
-        cplx u = make_double2((-dx * t.x * i90 + 11.0 * um2.x + 16.0 * um1.x) * i27,
-                              (-dx * t.y * i90 + 11.0 * um2.y + 16.0 * um1.y) * i27);
-        U[i] = u;
-        um2 = um1; um1 = u;
-        d0 = d1; d1 = d2; d2 = d3; d3 = d4;
-    }
-    int i = nx - 2;
-    {
-        cplx a = D[i - 2], b = D[i - 1], c0 = D[i], d = D[i + 1];
-        cplx t = make_double2(10.0 * a.x + 57.0 * b.x + 24.0 * c0.x - d.x, 10.0 * a.y + 57.0 * b.y + 24.0 * c0.y - d.y);
-        cplx u = make_double2((-dx * t.x + 33.0 * um2.x + 24.0 * um1.x) * i57, (-dx * t.y + 33.0 * um2.y + 24.0 * um1.y) * i57);
-        U[i] = u; um2 = um1; um1 = u;
-    }
-    i = nx - 1;
-    {
-        cplx t = rr(251.0, D[i], 646.0, D[i - 1], -264.0, D[i - 2], 106.0, D[i - 3], -19.0, D[i - 4]);
-        U[i] = make_double2((-dx * t.x + 720.0 * um1.x) * i720, (-dx * t.y + 720.0 * um1.y) * i720);
-    }
+    auto cb_ = [=](int i) -> double {
+        if (i <= 1 || i == n - 1) return 0.0;
+        if (i == n - 2) return -33.0 * i57;
+        return -11.0 * i27;
+    };
+    warp_rec2_fwd(Vl, r0, r1, lane, ca_, cb_);
+    __syncwarp();
+    for (int i = lane; i < n; i += 32)
+        if (i >= 1) out[i] = V[L.slot(i)];
 }
 
-// x-penta Poisson of poi_ux / poi_uz (loop_par.f:519-563, 641-685): one thread
-// per line (j >= 2, k >= 2); rhs formed on the fly, lusolver (penta_par.f:130-208).
-// sgn_d multiplies the derivative term, sgn_w the i k beta term; for poi_ux
-// rhs = -(D + vkb W) weights, for poi_uz rhs = (D - vkb W) weights.
+// poi_ux mode 0: ux(:, j, 0) from duydy by x integration, one warp per row j = 1..ny-2.
+__global__ void __launch_bounds__(64) k_ux_mode0(cplx* ux, const cplx* duydy, int nx, int ny, double dx) {
+    extern __shared__ cplx wsm[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int j = 1 + blockIdx.x * (blockDim.x >> 5) + wib;
+    if (j > ny - 2) return;
+    const WarpLine L{nx, WarpLine::chunk(nx), WarpLine::padded(nx)};
+    cplx* E = wsm + (size_t)wib * 64 * L.Sp;
+    cplx* V = E + 32 * L.Sp;
+    const cplx* D = duydy + (size_t)nx * j;
+    for (int i = lane; i < nx; i += 32) E[L.slot(i)] = D[i];
+    __syncwarp();
+    cplx* U = ux + (size_t)nx * j;
+    xint_line(E, V, L, lane, U[0], -dx, U);
+}
+
+// wz_wall: wall wz of mode k from r = v_kb wx - lapv by x integration, one warp per mode.
+__global__ void __launch_bounds__(64) k_wz_wall(cplx* wz, const cplx* wx, const cplx* lapv, int nx, int ny, int K, double dx,
+                                                double beta) {
+    extern __shared__ cplx wsm[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int k = blockIdx.x * (blockDim.x >> 5) + wib;
+    if (k >= K) return;
+    const WarpLine L{nx, WarpLine::chunk(nx), WarpLine::padded(nx)};
+    cplx* E = wsm + (size_t)wib * 64 * L.Sp;
+    cplx* V = E + 32 * L.Sp;
+    const double kb = (double)k * beta;
+    const cplx* WX = wx + (size_t)nx * ny * k;
+    const cplx* LV = lapv + (size_t)nx * k;
+    for (int i = lane; i < nx; i += 32) { cplx v = ikb(kb, WX[i]); cplx l = LV[i]; E[L.slot(i)] = make_double2(v.x - l.x, v.y - l.y); }
+    __syncwarp();
+    cplx* W = wz + (size_t)nx * ny * k;
+    xint_line(E, V, L, lane, W[0], dx, W);
+}
+
+// Pentadiagonal x solve with the LU of lhs5 (lusolver / lusolver_1,
+// penta_par.f:53-208) of mode k, rhs rows
+//   r_0 = boundary value, r_1 = c12 (e_0 + 10 e_1 + e_2),
+//   r_i = c8 (e_{i-1} + 5.5 e_i + e_{i+1}),  r_{n-2} = c12 (e_{n-1} + 10 e_{n-2} + e_{n-3}),
+//   r_{n-1} = rn,
+// with e in E; the solution (rows 1..n-1) goes to out.
+__device__ void penta_line(const cplx* E, cplx* V, const WarpLine& L, int lane, const double* lu, cplx r0v, cplx rn,
+                           double c12, double c8, cplx* out) {
+    const int n = L.n, r0 = lane * L.S, r1 = min(n, r0 + L.S);
+    auto e = [&](int i) { return E[L.slot(i)]; };
+    cplx* Vl = V + lane * L.Sp;
+    for (int i = r0; i < r1; i++) {
+        cplx v;
+        if (i == 0) v = r0v;
+        else if (i == 1) { cplx a = e(0), b = e(1), c = e(2); v = make_double2(c12 * (a.x + 10.0 * b.x + c.x), c12 * (a.y + 10.0 * b.y + c.y)); }
+        else if (i <= n - 3) { cplx a = e(i - 1), b = e(i), c = e(i + 1); v = make_double2(c8 * (a.x + 5.5 * b.x + c.x), c8 * (a.y + 5.5 * b.y + c.y)); }
+        else if (i == n - 2) { cplx a = e(n - 1), b = e(n - 2), c = e(n - 3); v = make_double2(c12 * (a.x + 10.0 * b.x + c.x), c12 * (a.y + 10.0 * b.y + c.y)); }
+        else v = rn;
+        Vl[i - r0] = v;
+    }
+    const double *L1 = lu, *L2 = lu + n, *IU3 = lu + 2 * n, *U4 = lu + 3 * n, *U5 = lu + 4 * n;
+    // forward y_i = r_i - l2_i y_{i-1} - l1_i y_{i-2}; row 0 is the boundary row
+    warp_rec2_fwd(Vl, r0, r1, lane, [=](int i) { return i == 0 ? 0.0 : L2[i]; }, [=](int i) { return i <= 1 ? 0.0 : L1[i]; });
+    // backward x_i = (y_i - u4_i x_{i+1} - u5_i x_{i+2}) / u3_i; row 0 keeps its value
+    warp_rec2_bwd(Vl, r0, r1, lane, [=](int i) { return i == 0 ? 0.0 : U4[i]; }, [=](int i) { return i == 0 ? 0.0 : U5[i]; },
+                  [=](int i) { return i == 0 ? 1.0 : IU3[i]; });
+    __syncwarp();
+    for (int i = lane; i < n; i += 32)
+        if (i >= 1) out[i] = V[L.slot(i)];
+}
+
+// x-penta Poisson of poi_ux / poi_uz (loop_par.f:519-563, 641-685), one warp
+// per line (j >= 1, k >= 1): e = D + s v_kb W, rhs scaled by g (ux: s = +1,
+// g = -1; uz: s = -1, g = +1); the last row is (g' D + v_kb W) / (k beta)^2.
 struct PentaArgs {
     const cplx* D;   // d2uydxdy or dwydx
     const cplx* W;   // wy or duydy
@@ -173,71 +254,31 @@ struct PentaArgs {
     int nx, ny, K, uz;
     double dxx, beta;
 };
-__global__ void k_penta_x(PentaArgs A) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    int nl = (A.ny - 1) * (A.K - 1);
-    if (t >= nl) return;
-    int j = 1 + t % (A.ny - 1);
-    int k = 1 + t / (A.ny - 1);
-    int n = A.nx;
+__global__ void __launch_bounds__(64) k_penta_x(PentaArgs A) {
+    extern __shared__ cplx wsm[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int t = blockIdx.x * (blockDim.x >> 5) + wib;
+    if (t >= (A.ny - 1) * (A.K - 1)) return;
+    const int j = 1 + t % (A.ny - 1), k = 1 + t / (A.ny - 1);
+    const int n = A.nx;
+    const WarpLine L{n, WarpLine::chunk(n), WarpLine::padded(n)};
+    cplx* E = wsm + (size_t)wib * 64 * L.Sp;
+    cplx* V = E + 32 * L.Sp;
     size_t base = (size_t)n * (j + (size_t)A.ny * k);
     const cplx* D = A.D + base;
     const cplx* W = A.W + base;
     cplx* O = A.out + base;
-    const double* L1 = A.lu + (size_t)k * 5 * n;  // lu(:,1)
-    const double* L2 = L1 + n;                    // lu(:,2)
-    const double* IU3 = L1 + 2 * n;               // 1/lu(:,3)
-    const double* U4 = L1 + 3 * n;
-    const double* U5 = L1 + 4 * n;
-    double kb = (double)k * A.beta;
-    double den = 1.0 / ((double)k * (double)k * A.beta * A.beta);
-    // combination D + s * vkb W, s = +1 (ux) or -1 (uz); overall sign g = -1 (ux) or +1 (uz)
-    double s = A.uz ? -1.0 : 1.0, g = A.uz ? 1.0 : -1.0;
-    auto comb = [&](cplx d, cplx w) { cplx v = ikb(kb, w); return make_double2(d.x + s * v.x, d.y + s * v.y); };
-    const double c12 = A.dxx / 12.0, c8 = 8.0 * A.dxx;
-    // forward: y(1) = rhs(1), y(2) = rhs(2) - l2 y(1), y(i) = rhs(i) - l1 y(i-2) - l2 y(i-1)
-    cplx y0 = O[0];  // rhs(1) = ux(1,j,k) / uz(1,j,k)
-    O[0] = y0;
-    cplx e0 = comb(D[0], W[0]), e1 = comb(D[1], W[1]), e2 = comb(D[2], W[2]);
-    cplx r1 = make_double2(g * c12 * (e0.x + 10.0 * e1.x + e2.x), g * c12 * (e0.y + 10.0 * e1.y + e2.y));
-    cplx y1 = make_double2(r1.x - L2[1] * y0.x, r1.y - L2[1] * y0.y);
-    O[1] = y1;
-    cplx ym2 = y0, ym1 = y1;
-    for (int i = 2; i <= n - 3; i++) {
-        cplx e3 = comb(D[i + 1], W[i + 1]);
-        cplx r = make_double2(g * c8 * (e1.x + 5.5 * e2.x + e3.x), g * c8 * (e1.y + 5.5 * e2.y + e3.y));
-        cplx y = make_double2(r.x - L1[i] * ym2.x - L2[i] * ym1.x, r.y - L1[i] * ym2.y - L2[i] * ym1.y);
-        O[i] = y;
-        ym2 = ym1; ym1 = y;
-        e1 = e2; e2 = e3;
+    const double kb = (double)k * A.beta;
+    const double s = A.uz ? -1.0 : 1.0, g = A.uz ? 1.0 : -1.0;
+    for (int i = lane; i < n; i += 32) {
+        cplx v = ikb(kb, W[i]), d = D[i];
+        E[L.slot(i)] = make_double2(d.x + s * v.x, d.y + s * v.y);
     }
-    {
-        int i = n - 2;
-        cplx a = comb(D[n - 1], W[n - 1]);  // e1=comb(i-1), e2 = comb(i)
-        cplx r = make_double2(g * c12 * (a.x + 10.0 * e2.x + e1.x), g * c12 * (a.y + 10.0 * e2.y + e1.y));
-        cplx y = make_double2(r.x - L1[i] * ym2.x - L2[i] * ym1.x, r.y - L1[i] * ym2.y - L2[i] * ym1.y);
-        O[i] = y;
-        ym2 = ym1; ym1 = y;
-        i = n - 1;
-        cplx v = ikb(kb, W[n - 1]);
-        cplx dn = D[n - 1];
-        cplx rn = A.uz ? make_double2((-dn.x + v.x) * den, (-dn.y + v.y) * den)
-                       : make_double2((v.x + dn.x) * den, (v.y + dn.y) * den);
-        cplx yn = make_double2(rn.x - L1[i] * ym2.x - L2[i] * ym1.x, rn.y - L1[i] * ym2.y - L2[i] * ym1.y);
-        // backward: x(n) = y(n)/lu3, x(n-1) = (y - lu4 x(n))/lu3, x(i) = (y - lu4 x(i+1) - lu5 x(i+2))/lu3
-        cplx xn = make_double2(yn.x * IU3[n - 1], yn.y * IU3[n - 1]);
-        cplx xm = make_double2((y.x - U4[n - 2] * xn.x) * IU3[n - 2], (y.y - U4[n - 2] * xn.y) * IU3[n - 2]);
-        O[n - 1] = xn; O[n - 2] = xm;
-        cplx xp2 = xn, xp1 = xm;
-        for (int ii = n - 3; ii >= 1; ii--) {
-            cplx yy = O[ii];
-            cplx x = make_double2((yy.x - U4[ii] * xp1.x - U5[ii] * xp2.x) * IU3[ii],
-                                  (yy.y - U4[ii] * xp1.y - U5[ii] * xp2.y) * IU3[ii]);
-            O[ii] = x;
-            xp2 = xp1; xp1 = x;
-        }
-        // i = 1 keeps ux(1) (lu(1,3) = 1, upper entries 0)
-    }
+    __syncwarp();
+    const double den = 1.0 / ((double)k * (double)k * A.beta * A.beta);
+    cplx v = ikb(kb, W[n - 1]), dn = D[n - 1];
+    cplx rn = A.uz ? make_double2((-dn.x + v.x) * den, (-dn.y + v.y) * den) : make_double2((v.x + dn.x) * den, (v.y + dn.y) * den);
+    penta_line(E, V, L, lane, A.lu + (size_t)k * 5 * n, O[0], rn, g * (A.dxx / 12.0), g * (8.0 * A.dxx), O);
 }
 
 // lapv (loop_par.f:194-205) for every (i, k).
@@ -269,129 +310,64 @@ __global__ void k_dwydy_wall(cplx* out, const cplx* wy, const double* w, int nx,
     out[t] = make_double2(invdy * acc.x, invdy * acc.y);
 }
 
-// wx_wall (loop_par.f:174-255): per mode k >= 2, d2wy/dxdy by explicit
-// stencils, then the x-penta solve with lusolver_1 (penta_par.f:53-127).
-// One thread per mode.
-__global__ void k_wx_wall(cplx* wx, const cplx* dwdy, const cplx* lapv, const double* lu_all, int nx, int ny, int K,
-                          double dx, double dxx, double beta) {
-    int k = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+// wx_wall (loop_par.f:174-255): per mode k >= 1, d2wy/dxdy by explicit
+// stencils, then the x-penta solve with the LU of lhs5 (lusolver_1,
+// penta_par.f:53-127); one warp per mode.
+__global__ void __launch_bounds__(64) k_wx_wall(cplx* wx, const cplx* dwdy, const cplx* lapv, const double* lu_all, int nx,
+                                                int ny, int K, double dx, double dxx, double beta) {
+    extern __shared__ cplx wsm[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int k = 1 + blockIdx.x * (blockDim.x >> 5) + wib;
     if (k >= K) return;
     const int n = nx;
+    const WarpLine L{n, WarpLine::chunk(n), WarpLine::padded(n)};
+    cplx* E = wsm + (size_t)wib * 64 * L.Sp;
+    cplx* V = E + 32 * L.Sp;
     const cplx* dw = dwdy + (size_t)nx * k;
     const cplx* LV = lapv + (size_t)nx * k;
     cplx* WX = wx + (size_t)nx * ny * k;  // row j = 1
-    const double* L1 = lu_all + (size_t)k * 5 * n;
-    const double* L2 = L1 + n;
-    const double* IU3 = L1 + 2 * n;
-    const double* U4 = L1 + 3 * n;
-    const double* U5 = L1 + 4 * n;
-    double kb = (double)k * beta;
-    double idx6 = 1.0 / 6.0 / dx, idx60 = 1.0 / 60.0 / dx, idx12 = 1.0 / 12.0 / dx, idx2 = 1.0 / 2.0 / dx;
+    const double kb = (double)k * beta;
+    const double idx6 = 1.0 / 6.0 / dx, idx60 = 1.0 / 60.0 / dx, idx12 = 1.0 / 12.0 / dx, idx2 = 1.0 / 2.0 / dx;
     auto d2 = [&](int i) -> cplx {  // d2wydxdy(i), 0-based i
         if (i >= 3 && i <= n - 4) {
             cplx a = dw[i + 1], b = dw[i - 1], c = dw[i - 2], d = dw[i + 2], e = dw[i + 3], f = dw[i - 3];
             return make_double2((45.0 * (a.x - b.x) + 9.0 * (c.x - d.x) + e.x - f.x) * idx60,
                                 (45.0 * (a.y - b.y) + 9.0 * (c.y - d.y) + e.y - f.y) * idx60);
         }
-        const double* cw; int b0, e; double sc;
-        static const double W0[7] = {-14.7, 36.0, -45.0, 40.0, -22.5, 7.2, -1.0};
-        static const double W1[7] = {-1.0, -7.7, 15.0, -10.0, 5.0, -1.5, 0.2};
-        static const double W2[7] = {0.2, -2.4, -3.5, 8.0, -3.0, 0.8, -0.1};
-        if (i == 0) { cw = W0; b0 = 0; e = 7; sc = idx6; }
-        else if (i == 1) { cw = W1; b0 = 0; e = 7; sc = idx6; }
-        else if (i == 2) { cw = W2; b0 = 0; e = 7; sc = idx6; }
-        else if (i == n - 3) {
+        if (i == n - 3) {
             cplx a = dw[n - 5], b = dw[n - 4], c = dw[n - 2], d = dw[n - 1];
             return make_double2((a.x - 8.0 * b.x + 8.0 * c.x - d.x) * idx12, (a.y - 8.0 * b.y + 8.0 * c.y - d.y) * idx12);
-        } else if (i == n - 2) {
+        }
+        if (i == n - 2) {
             cplx a = dw[n - 1], b = dw[n - 2], c = dw[n - 3], d = dw[n - 4];
             return make_double2((2.0 * a.x + 3.0 * b.x - 6.0 * c.x + d.x) * idx6, (2.0 * a.y + 3.0 * b.y - 6.0 * c.y + d.y) * idx6);
-        } else {
+        }
+        if (i == n - 1) {
             cplx a = dw[n - 1], b = dw[n - 2], c = dw[n - 3];
             return make_double2((3.0 * a.x - 4.0 * b.x + c.x) * idx2, (3.0 * a.y - 4.0 * b.y + c.y) * idx2);
         }
+        const double W0[7] = {-14.7, 36.0, -45.0, 40.0, -22.5, 7.2, -1.0};
+        const double W1[7] = {-1.0, -7.7, 15.0, -10.0, 5.0, -1.5, 0.2};
+        const double W2[7] = {0.2, -2.4, -3.5, 8.0, -3.0, 0.8, -0.1};
+        const double* cw = (i == 0) ? W0 : (i == 1) ? W1 : W2;
         cplx acc = make_double2(0, 0);
-        for (int m = 0; m < e; m++) { acc.x += cw[m] * dw[b0 + m].x; acc.y += cw[m] * dw[b0 + m].y; }
-        return make_double2(acc.x * sc, acc.y * sc);
+        for (int m = 0; m < 7; m++) { acc.x += cw[m] * dw[m].x; acc.y += cw[m] * dw[m].y; }
+        return make_double2(acc.x * idx6, acc.y * idx6);
     };
-    // combination -d2 + vkb lapv
-    auto comb = [&](int i) { cplx a = d2(i); cplx v = ikb(kb, LV[i]); return make_double2(-a.x + v.x, -a.y + v.y); };
-    const double c12 = dxx / 12.0, c8 = 8.0 * dxx;
-    // forward (lusolver_1 order: - l2 y(i-1) - l1 y(i-2))
-    cplx y0 = WX[0];
-    WX[0] = y0;
-    cplx e0 = comb(0), e1 = comb(1), e2 = comb(2);
-    cplx r1 = make_double2(c12 * (e0.x + 10.0 * e1.x + e2.x), c12 * (e0.y + 10.0 * e1.y + e2.y));
-    cplx y1 = make_double2(r1.x - L2[1] * y0.x, r1.y - L2[1] * y0.y);
-    WX[1] = y1;
-    cplx ym2 = y0, ym1 = y1;
-    for (int i = 2; i <= n - 3; i++) {
-        cplx e3 = comb(i + 1);
-        cplx r = make_double2(c8 * (e1.x + 5.5 * e2.x + e3.x), c8 * (e1.y + 5.5 * e2.y + e3.y));
-        cplx y = make_double2(r.x - L2[i] * ym1.x - L1[i] * ym2.x, r.y - L2[i] * ym1.y - L1[i] * ym2.y);
-        WX[i] = y;
-        ym2 = ym1; ym1 = y;
-        e1 = e2; e2 = e3;
+    for (int i = lane; i < n; i += 32) {
+        cplx a = d2(i), v = ikb(kb, LV[i]);
+        E[L.slot(i)] = make_double2(-a.x + v.x, -a.y + v.y);
     }
-    int i = n - 2;
-    cplx a = comb(n - 1);
-    cplx r = make_double2(c12 * (a.x + 10.0 * e2.x + e1.x), c12 * (a.y + 10.0 * e2.y + e1.y));
-    cplx y = make_double2(r.x - L2[i] * ym1.x - L1[i] * ym2.x, r.y - L2[i] * ym1.y - L1[i] * ym2.y);
-    WX[i] = y; ym2 = ym1; ym1 = y;
-    i = n - 1;
+    __syncwarp();
+    const double den = 1.0 / ((double)k * (double)k * beta * beta);
     cplx dd = d2(n - 1), vv = ikb(kb, LV[n - 1]);
-    double den = 1.0 / ((double)k * (double)k * beta * beta);
     cplx rn = make_double2((dd.x - vv.x) * den, (dd.y - vv.y) * den);
-    cplx yn = make_double2(rn.x - L2[i] * ym1.x - L1[i] * ym2.x, rn.y - L2[i] * ym1.y - L1[i] * ym2.y);
-    cplx xn = make_double2(yn.x * IU3[n - 1], yn.y * IU3[n - 1]);
-    cplx xm = make_double2((y.x - U4[n - 2] * xn.x) * IU3[n - 2], (y.y - U4[n - 2] * xn.y) * IU3[n - 2]);
-    WX[n - 1] = xn; WX[n - 2] = xm;
-    cplx xp2 = xn, xp1 = xm;
-    for (int ii = n - 3; ii >= 1; ii--) {
-        cplx yy = WX[ii];
-        cplx x = make_double2((yy.x - U4[ii] * xp1.x - U5[ii] * xp2.x) * IU3[ii], (yy.y - U4[ii] * xp1.y - U5[ii] * xp2.y) * IU3[ii]);
-        WX[ii] = x;
-        xp2 = xp1; xp1 = x;
-    }
+    penta_line(E, V, L, lane, lu_all + (size_t)k * 5 * n, WX[0], rn, dxx / 12.0, 8.0 * dxx, WX);
 }
 
-// wz_wall (loop_par.f:361-425): wall wz by implicit x integration, one thread per mode.
-__global__ void k_wz_wall(cplx* wz, const cplx* wx, const cplx* lapv, int nx, int ny, int K, double dx, double beta) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= K) return;
-    double kb = (double)k * beta;
-    const cplx* WX = wx + (size_t)nx * ny * k;
-    const cplx* LV = lapv + (size_t)nx * k;
-    cplx* W = wz + (size_t)nx * ny * k;
-    auto R = [&](int i) { cplx v = ikb(kb, WX[i]); cplx l = LV[i]; return make_double2(v.x - l.x, v.y - l.y); };
-    const double i720 = 1.0 / 720.0, i27 = 1.0 / 27.0, i90 = 1.0 / 90.0, i57 = 1.0 / 57.0;
-    cplx r0 = R(0), r1 = R(1), r2 = R(2), r3 = R(3), r4 = R(4);
-    cplx w0 = W[0];
-    cplx w1 = make_double2((dx * (251.0 * r0.x + 646.0 * r1.x - 264.0 * r2.x + 106.0 * r3.x - 19.0 * r4.x) + 720.0 * w0.x) * i720,
-                           (dx * (251.0 * r0.y + 646.0 * r1.y - 264.0 * r2.y + 106.0 * r3.y - 19.0 * r4.y) + 720.0 * w0.y) * i720);
-    W[1] = w1;
-    cplx wm2 = w0, wm1 = w1;
-    cplx a0 = r0, a1 = r1, a2 = r2, a3 = r3;
-    for (int i = 2; i <= nx - 3; i++) {
-        cplx a4 = R(i + 2);
-        cplx w = make_double2((dx * (281.0 * a0.x + 2056.0 * a1.x + 1176.0 * a2.x - 104.0 * a3.x + 11.0 * a4.x) * i90 +
-                               11.0 * wm2.x + 16.0 * wm1.x) * i27,
-                              (dx * (281.0 * a0.y + 2056.0 * a1.y + 1176.0 * a2.y - 104.0 * a3.y + 11.0 * a4.y) * i90 +
-                               11.0 * wm2.y + 16.0 * wm1.y) * i27);
-        W[i] = w;
-        wm2 = wm1; wm1 = w;
-        a0 = a1; a1 = a2; a2 = a3; a3 = a4;
-    }
-    int i = nx - 2;
-    cplx b0 = R(i - 2), b1 = R(i - 1), b2 = R(i), b3 = R(i + 1);
-    cplx w = make_double2((dx * (10.0 * b0.x + 57.0 * b1.x + 24.0 * b2.x - b3.x) + 33.0 * wm2.x + 24.0 * wm1.x) * i57,
-                          (dx * (10.0 * b0.y + 57.0 * b1.y + 24.0 * b2.y - b3.y) + 33.0 * wm2.y + 24.0 * wm1.y) * i57);
-    W[i] = w; wm2 = wm1; wm1 = w;
-    i = nx - 1;
-    cplx c0 = R(i), c1 = R(i - 1), c2 = R(i - 2), c3 = R(i - 3), c4 = R(i - 4);
-    W[i] = make_double2((dx * (251.0 * c0.x + 646.0 * c1.x - 264.0 * c2.x + 106.0 * c3.x - 19.0 * c4.x) + 720.0 * wm1.x) * i720,
-                        (dx * (251.0 * c0.y + 646.0 * c1.y - 264.0 * c2.y + 106.0 * c3.y - 19.0 * c4.y) + 720.0 * wm1.y) * i720);
-}
+// Shared memory of the warp-per-line x kernels (two line buffers per warp).
+constexpr int XW_WARPS = 2;
+size_t xw_smem(int nx) { return (size_t)XW_WARPS * 64 * WarpLine::padded(nx) * sizeof(cplx); }
 
 // ts2d_pert / ts3d_pert (main_par.f:1613-1685) for each forced mode.
 struct PertArgs {
@@ -519,7 +495,9 @@ int tb_poi_ux_k(tb_ctx* c, cplx* duydy) {
     int r;
     YJob yj[1] = {{c->uy, duydy, YOP_D1FV}};
     if ((r = tb_launch_ylines(c, yj, 1))) return r;
-    k_ux_mode0<<<tb_blocks(c->g.ny, 64), 64, 0, c->stream>>>(c->ux, duydy, c->g.nx, c->g.ny, c->cfg.dx);
+    size_t sm = xw_smem(c->g.nx);
+    TB_CUDA(cudaFuncSetAttribute(k_ux_mode0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_ux_mode0<<<tb_blocks(c->g.ny - 2, XW_WARPS), 32 * XW_WARPS, sm, c->stream>>>(c->ux, duydy, c->g.nx, c->g.ny, c->cfg.dx);
     TB_CHECK_LAUNCH(c);
     if (c->g.K < 2) return TB_OK;
     cplx* d2 = c->tmp[13];
@@ -528,7 +506,8 @@ int tb_poi_ux_k(tb_ctx* c, cplx* duydy) {
     PentaArgs A{d2, c->wy, c->ux, c->px.lu, c->g.nx, c->g.ny, c->g.K, 0, c->cfg.dx * c->cfg.dx, c->cfg.beta};
     cudaEvent_t ps = nullptr;
     if ((r = tb_prof_begin(c, PROF_PENTA, &ps))) return r;
-    k_penta_x<<<tb_blocks((size_t)(c->g.ny - 1) * (c->g.K - 1), 128), 128, 0, c->stream>>>(A);
+    TB_CUDA(cudaFuncSetAttribute(k_penta_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_penta_x<<<tb_blocks((size_t)(c->g.ny - 1) * (c->g.K - 1), XW_WARPS), 32 * XW_WARPS, sm, c->stream>>>(A);
     TB_CHECK_LAUNCH(c);
     return tb_prof_end(c, PROF_PENTA, ps);
 }
@@ -539,21 +518,17 @@ int tb_poi_uz_k(tb_ctx* c, const cplx* duydy) {
     XJob xj[1] = {{c->wy, dwydx, XOP_D1}};
     if ((r = tb_launch_xlines(c, xj, 1))) return r;
     PentaArgs A{dwydx, duydy, c->uz, c->px.lu, c->g.nx, c->g.ny, c->g.K, 1, c->cfg.dx * c->cfg.dx, c->cfg.beta};
-    k_penta_x<<<tb_blocks((size_t)(c->g.ny - 1) * (c->g.K - 1), 128), 128, 0, c->stream>>>(A);
+    size_t sm = xw_smem(c->g.nx);
+    cudaEvent_t ps = nullptr;
+    if ((r = tb_prof_begin(c, PROF_PENTA, &ps))) return r;
+    TB_CUDA(cudaFuncSetAttribute(k_penta_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_penta_x<<<tb_blocks((size_t)(c->g.ny - 1) * (c->g.K - 1), XW_WARPS), 32 * XW_WARPS, sm, c->stream>>>(A);
     TB_CHECK_LAUNCH(c);
-    return TB_OK;
+    return tb_prof_end(c, PROF_PENTA, ps);
 }
 int tb_wx_wall_k(tb_ctx* c, cplx* lapv) {
-    const double* wat = c->coefs.data() + 100 + 24 * c->g.msh - 17;  // w_at_w_coef(9)
-    const double* dwy = wat + 9;                                       // dwydy_coef(8)
-    // coefficients live on the host; stage them through a small device buffer
-    static thread_local double* dcoef = nullptr;
-    static thread_local int dcoef_dev = -1;
-    if (!dcoef || dcoef_dev != c->device) {
-        TB_CUDA(cudaMalloc(&dcoef, 17 * sizeof(double)));
-        dcoef_dev = c->device;
-    }
-    TB_CUDA(cudaMemcpyAsync(dcoef, wat, 17 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    const double* wat = c->coefs.data() + 100 + 24 * c->g.msh - 17;  // w_at_w_coef(9) on the host
+    const double* dcoef = c->wcoef;   // device copy of w_at_w_coef(9), dwydy_coef(8)
     double dyy = c->cfg.dy * c->cfg.dy;
     unsigned nb = tb_blocks((size_t)c->g.nx * c->g.K, 128);
     k_lapv<<<nb, 128, 0, c->stream>>>(lapv, c->uy, c->d2uydx2, c->k2b2, dcoef, c->g.nx, c->g.ny, c->g.K,
@@ -563,14 +538,19 @@ int tb_wx_wall_k(tb_ctx* c, cplx* lapv) {
     cplx* dw = c->tmp[15];
     k_dwydy_wall<<<nb, 128, 0, c->stream>>>(dw, c->wy, dcoef + 9, c->g.nx, c->g.ny, c->g.K, 1.0 / c->cfg.dy);
     TB_CHECK_LAUNCH(c);
-    k_wx_wall<<<tb_blocks(c->g.K - 1, 32), 32, 0, c->stream>>>(c->wx, dw, lapv, c->px.lu, c->g.nx, c->g.ny, c->g.K, c->cfg.dx,
-                                                               c->cfg.dx * c->cfg.dx, c->cfg.beta);
+    size_t sm = xw_smem(c->g.nx);
+    TB_CUDA(cudaFuncSetAttribute(k_wx_wall, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_wx_wall<<<tb_blocks(c->g.K - 1, XW_WARPS), 32 * XW_WARPS, sm, c->stream>>>(c->wx, dw, lapv, c->px.lu, c->g.nx, c->g.ny,
+                                                                                 c->g.K, c->cfg.dx, c->cfg.dx * c->cfg.dx,
+                                                                                 c->cfg.beta);
     TB_CHECK_LAUNCH(c);
-    (void)dwy;
     return TB_OK;
 }
 int tb_wz_wall_k(tb_ctx* c, const cplx* lapv) {
-    k_wz_wall<<<tb_blocks(c->g.K, 32), 32, 0, c->stream>>>(c->wz, c->wx, lapv, c->g.nx, c->g.ny, c->g.K, c->cfg.dx, c->cfg.beta);
+    size_t sm = xw_smem(c->g.nx);
+    TB_CUDA(cudaFuncSetAttribute(k_wz_wall, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_wz_wall<<<tb_blocks(c->g.K, XW_WARPS), 32 * XW_WARPS, sm, c->stream>>>(c->wz, c->wx, lapv, c->g.nx, c->g.ny, c->g.K,
+                                                                             c->cfg.dx, c->cfg.beta);
     TB_CHECK_LAUNCH(c);
     return TB_OK;
 }
