@@ -1,21 +1,24 @@
 """Benchmark: grid-point RK4 steps per second of the trans_bl stage on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed|plain]
-                    [--impl ours|reference]
+                    [--impl ours|reference] [--workload config2|small]
 
 Workload: the 3D Blasius/TS case nx=1025, ny=193, 32 Fourier modes (P=64),
-4-level multigrid, Poisson residual 1e-10 (synthetic inputs: Falkner-Skan
-base flow, generated coefficient tables, seeded wall-forcing phases).
+4-level multigrid, Poisson max-defect 1e-10, 1024 steps per forcing period
+(synthetic inputs: Falkner-Skan base flow, generated coefficient tables,
+seeded wall-forcing phases, a seeded smooth disturbance of every field).
 One step = one RK4 time step (four stages) over the whole domain.
 
-value  : Mpt-steps/s = nx*ny*kfour*steps / device time, all ranks summed
-         (replicas: every rank advances its own simulation; no collective).
-e2e    : the same through the C ABI with the state uploaded from pinned host
-         memory before and read back after every step.
-The CPU baseline is the oracle (C++ restatement of the reference CPU path)
-timed on one RK stage of the same workload on the host cores.
-With --impl reference the whole line times that restatement instead, with
-all host threads, one RK stage per sample.
+value        : Mpt-steps/s = nx*ny*kfour*steps / device time, summed over
+               ranks (replicas: every rank advances its own simulation).
+e2e          : the same through the C ABI with the six state fields copied
+               from pinned host memory before and back after every step.
+plain_fp64   : (with --form mixed) the plain FP64 form timed in the same run
+               from the same state, its mean V-cycles, the step-level byte
+               model, and the mixed-vs-plain field error after two steps.
+cpu_baseline : the oracle (C++ restatement of the reference CPU path) timed
+               on one RK stage of the same state on all host threads.
+With --impl reference the whole line times that restatement instead.
 """
 import argparse
 import json
@@ -31,6 +34,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 METRIC = "Mpt-steps/s (1 GB300): batched+mixed+learned vs plain FP64 at <=1e-6 rel err"
+NAMES = ("ux", "uy", "uz", "wx", "wy", "wz")
 
 
 def parse():
@@ -41,14 +45,15 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--form", default="mixed", choices=["mixed", "plain"],
                    help="mixed: FP32 multigrid inside FP64 defect correction (default); plain: the reference's FP64 SOR")
-    p.add_argument("--workload", default="config2", choices=["config2", "small"],
-                   help="small: 129x65x8 grid for profiler captures")
+    p.add_argument("--workload", default="config2", choices=["config2", "medium", "small"],
+                   help="medium: 513x193x16, small: 129x65x8 grids for profiler captures")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     return p.parse_args()
 
 
-def dist_init(n):
+def dist_init():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if world > 1:
@@ -132,57 +137,132 @@ def workload(form):
     prec = api.FORM_MIXED if form == "mixed" else api.FORM_PLAIN_FP64
     if WORKLOAD["name"] == "small":
         return configs.small(nx=129, ny=65, kfour=8, kphys=16, msh=3, tol=1e-10, precision=prec)
+    if WORKLOAD["name"] == "medium":
+        return configs.blasius_ts_config(513, 193, 16, 32, 4, steps_per_period=1024, amp2d=1e-4, amp3d=1e-5,
+                                         tol=1e-10, precision=prec)
     return configs.config2(tol=1e-10, precision=prec)
 
 
-def cpu_stage_sample(cfg, coefs, base, state, threads, t):
-    """Time one RK stage of the oracle on the given state (seconds)."""
+def workload_name(cfg):
+    return "blasius_ts_3d nx=%d ny=%d kfour=%d kphys=%d msh=%d tol=1e-10 steps_per_period=%d" % (
+        cfg.nx, cfg.ny, cfg.kfour, cfg.kphys, cfg.msh, cfg.stpp)
+
+
+def start_state(cfg, base):
+    from trans_bl_gb300 import configs
+    return configs.disturbed_state(cfg, base, np.random.default_rng(5))
+
+
+def cpu_stage_seconds(cfg, coefs, base, state, threads, t):
+    """One RK stage of the oracle on the given state, on `threads` host threads (s)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as ora
-    os.environ["OMP_NUM_THREADS"] = str(threads)
+    used = ora.set_threads(threads)
     o = ora.Oracle(cfg, coefs, base)
-    if state is not None:
-        o.put_state(state)
+    o.put_state(state)
     t0 = time.perf_counter()
     o.rk_stage(1, t)
-    return time.perf_counter() - t0
+    el = time.perf_counter() - t0
+    o.close()
+    return el, used
 
 
-def run_reference(args, rank, world, dist):
+def run_reference(args, rank, world):
     """Reference arm: the CPU restatement of the reference path, all host threads."""
     if rank != 0:
         return
     from trans_bl_gb300 import configs
     cfg = workload("plain")
     coefs, base = configs.setup_inputs(cfg)
+    st = start_state(cfg, base)
     threads = os.cpu_count() or 1
     pts = cfg.nx * cfg.ny * cfg.kfour
     warm = min(args.warmup, 1)
     steps = max(1, min(args.steps, 2))
-    for w in range(warm):
-        cpu_stage_sample(cfg, coefs, base, None, threads, cfg.stpp + 1)
-    times = [cpu_stage_sample(cfg, coefs, base, None, threads, cfg.stpp + 1) for _ in range(steps)]
-    ms_per_step = 4.0 * 1e3 * float(np.mean(times))
+    used = threads
+    for _ in range(warm):
+        _, used = cpu_stage_seconds(cfg, coefs, base, st, threads, cfg.stpp + 1)
+    times = []
+    for _ in range(steps):
+        el, used = cpu_stage_seconds(cfg, coefs, base, st, threads, cfg.stpp + 1)
+        times.append(el)
+    ms_per_step = 4.0 * 1e3 * float(np.median(times))
     value = pts / (ms_per_step * 1e-3) / 1e6
-    sample = "one RK stage (of four) of the nx=1025 ny=193 K=32 step from the initial state, %d samples" % steps
+    sample = ("one RK stage (of four) of the nx=1025 ny=193 K=32 step from the benchmark's start state, "
+              "median of %d samples; per-step time = 4 x stage" % steps)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpt-steps/s", "n_gpus": world,
             "steps": steps, "warmup": warm, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "blasius_ts_3d nx=1025 ny=193 kfour=32 kphys=64 msh=4 tol=1e-10",
-                       "form": "reference CPU path (C++ restatement, OpenMP over modes and lines)"},
-            "cpu_baseline": {"value": value, "unit": "Mpt-steps/s", "cores": threads, "kind": "port",
-                             "sample": sample},
+            "config": {"workload": workload_name(cfg),
+                       "form": "reference CPU path (C++ restatement, OpenMP over lines and modes)"},
+            "cpu_baseline": {"value": value, "unit": "Mpt-steps/s", "cores": used, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "Mpt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def C_stream(ctx):
+    import ctypes as C
+    p = C.c_void_p()
+    ctx.lib.tb_stream(ctx.h, C.byref(p))
+    return p.value or 0
+
+
+def timed_steps(ctx, t, steps):
+    """Device time (ms) of `steps` RK4 steps, CUDA events on the context stream."""
+    import torch
+    ext = torch.cuda.ExternalStream(C_stream(ctx))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.synchronize()
+    ev0.record(ext)
+    for q in range(steps):
+        ctx.step(t + q)
+    ev1.record(ext)
+    ev1.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def step_bytes_model(nv):
+    """Bytes per grid point per RK4 step of the minimal-pass model for a fused
+    single-GPU dataflow: 16 B x (4 stages x 62 passes + 6 filter passes
+    + 4 stages x 26.4 passes per V-cycle x nV V-cycles)."""
+    return 16.0 * (4 * 62 + 6 + 4 * 26.4 * nv)
+
+
+def plain_comparison(coefs, base, mixed_state2, t0, hbm_peak):
+    """Plain FP64 form from the same start: step time, V-cycles, field error."""
+    from trans_bl_gb300 import api
+    cfg = workload("plain")
+    ctx = api.Context(cfg, coefs, base)
+    ctx.put_state(start_state(cfg, base))
+    ms1 = timed_steps(ctx, t0, 1)
+    nv1 = np.mean(ctx.poisson_stats()["vcycles"][:cfg.kfour])
+    ms2 = timed_steps(ctx, t0 + 1, 1)
+    nv2 = np.mean(ctx.poisson_stats()["vcycles"][:cfg.kfour])
+    sp = ctx.get_state()
+    err = {n: float(np.max(np.abs(mixed_state2[n] - sp[n])) / max(np.max(np.abs(sp[n])), 1e-300)) for n in NAMES}
+    ctx.close()
+    pts = cfg.nx * cfg.ny * cfg.kfour
+    ms = min(ms1, ms2)
+    nv = float(0.5 * (nv1 + nv2))
+    value = pts / (ms * 1e-3) / 1e6
+    B = step_bytes_model(nv)
+    return {"value": value, "unit": "Mpt-steps/s", "ms_per_step": ms, "steps": 2,
+            "mean_vcycles_per_mode_last_solve": nv,
+            "step_bytes_per_point_model": B,
+            "step_roofline": {"bound": "hbm", "achieved": value * 1e6 * B / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                              "frac": value * 1e6 * B / 1e9 / hbm_peak},
+            "mixed_vs_plain_rel_err_after_2_steps": err,
+            "max_rel_err": max(err.values())}
 
 
 def main():
     args = parse()
     WORKLOAD["name"] = args.workload
-    rank, world, dist = dist_init(args.gpus)
+    rank, world, dist = dist_init()
     if args.impl == "reference":
-        run_reference(args, rank, world, dist)
+        run_reference(args, rank, world)
         return
+    import torch
     from trans_bl_gb300 import api, configs
     form = args.form
     cfg = workload(form)
@@ -191,94 +271,81 @@ def main():
     pts = cfg.nx * cfg.ny * cfg.kfour
     # start from a disturbed state past the one-period forcing ramp, so every
     # mode carries a disturbance and every solve does work
-    ctx.put_state(configs.disturbed_state(cfg, base, np.random.default_rng(5)))
-    t = cfg.stpp + 1
-    for _ in range(max(3, args.warmup)):
+    t0 = cfg.stpp + 1
+    ctx.put_state(start_state(cfg, base))
+    t = t0
+    state2 = None
+    for q in range(max(3, args.warmup)):
         ctx.step(t)
         t += 1
+        if q == 1:
+            state2 = ctx.get_state()
     ctx.synchronize()
-    # timed region: device events on the library stream
-    import torch
-    stream_ptr = C_stream(ctx)
-    ext = torch.cuda.ExternalStream(stream_ptr)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = ctx.launch_count()
     ctx.profile(True)
     barrier(dist)
     torch.cuda.synchronize()
     with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-        ev0.record(ext)
-        for _ in range(args.steps):
-            ctx.step(t)
-            t += 1
-        ev1.record(ext)
-        ev1.synchronize()
+        ms = timed_steps(ctx, t, args.steps)
+    t += args.steps
     torch.cuda.synchronize()
     barrier(dist)
-    ms = ev0.elapsed_time(ev1)
     launches = ctx.launch_count() - launches0
-    sor_ms, sor_n = ctx.profile_read("sor")
-    poi_ms, poi_n = ctx.profile_read("poi_uy")
-    stage_ms, stage_n = ctx.profile_read("stage")
-    nl_ms, nl_n = ctx.profile_read("nlterms")
-    x_ms, x_n = ctx.profile_read("xlines")
-    def_ms, def_n = ctx.profile_read("defect")
-    r0_ms, r0_n = ctx.profile_read("relax0")
+    fam = {f: ctx.profile_read(f) for f in ("sor", "poi_uy", "stage", "nlterms", "xlines", "ylines", "penta", "defect",
+                                            "relax0")}
     ctx.profile(False)
     ms_max = max_over_ranks(dist, ms)
     ms_per_step = ms_max / args.steps
     value = world * pts * args.steps / (ms_max * 1e-3) / 1e6
-    # roofline of the dominant kernel family
     hbm_peak, peak_kind = peaks()
     stats = ctx.poisson_stats()
     if form == "plain":
         # line-SOR: per point and sweep, read fc and sc, write fc (3 x 16 B)
-        sweeps_pts = sor_points_per_launch(cfg)
-        bytes_per_launch = 48.0 * sweeps_pts
-        dom = {"kernel": "k_sor (lexicographic y-line SOR, one CTA per mode)", "ms": sor_ms, "launches": sor_n}
-        achieved = bytes_per_launch / (sor_ms * 1e-3 / max(sor_n, 1)) / 1e9 if sor_n else 0.0
+        bytes_per_launch = 48.0 * sor_points_per_launch(cfg)
+        r_ms, r_n = fam["sor"]
+        kernel = "k_sor (lexicographic y-line SOR, one CTA per mode)"
     else:
         # finest-level coloured y-line relaxation, FP32 complex (8 B): per
         # sweep (4 launches) every interior point reads r once, writes e once
         # and its e is read by the lines of the two other colours (2 x 8 B)
         bytes_per_launch = 32.0 * cfg.kfour * cfg.ny * (cfg.nx - 2) / 4.0
-        dom = {"kernel": "k_relax (finest level, one warp per y-line and mode)", "ms": r0_ms, "launches": r0_n}
-        achieved = bytes_per_launch / (r0_ms * 1e-3 / max(r0_n, 1)) / 1e9 if r0_n else 0.0
-    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_kind,
-            "kernel": dom["kernel"], "kernel_ms_total": dom["ms"], "kernel_launches": dom["launches"],
-            "share_of_step": dom["ms"] / ms if ms > 0 else None}
+        r_ms, r_n = fam["relax0"]
+        kernel = "k_relax (finest level, one warp per y-line and mode)"
+    achieved = bytes_per_launch / (r_ms * 1e-3 / max(r_n, 1)) / 1e9 if r_n else 0.0
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+            "traffic": None, "peak_source": peak_kind, "kernel": kernel,
+            "algorithmic_bytes_per_launch": bytes_per_launch, "kernel_ms_total": r_ms, "kernel_launches": r_n,
+            "share_of_step": r_ms / ms if ms > 0 else None}
     line = {"metric": METRIC, "value": value, "unit": "Mpt-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == "plain" else "f64+f32",
-            "data": "synthetic (Falkner-Skan base flow, generated coefficients, seeded TS forcing phases)",
-            "config": {"workload": "blasius_ts_3d nx=%d ny=%d kfour=%d kphys=%d msh=%d tol=1e-10 steps_per_period=%d" % (
-                           cfg.nx, cfg.ny, cfg.kfour, cfg.kphys, cfg.msh, cfg.stpp),
-                       "form": form, "replicas": world, "l2": "working set ~4 GB > L2 (129 MB)",
+            "data": "synthetic (Falkner-Skan base flow, generated coefficients, seeded TS forcing phases, "
+                    "seeded smooth disturbance)",
+            "config": {"workload": workload_name(cfg), "form": form, "replicas": world,
+                       "l2": "inputs larger than L2: working set ~5 GB vs 129 MB L2",
                        "start": "disturbed state (1e-3) past the forcing ramp",
                        "iterations_per_mode_last_solve": float(np.mean(stats["vcycles"][:cfg.kfour]))},
             "roofline": roof, "gpu_launches": launches,
-            "breakdown_ms": {"stage": stage_ms, "poi_uy": poi_ms, "relax_sweeps": sor_ms, "relax_finest": r0_ms,
-                             "fp64_defect": def_ms, "nlterms": nl_ms, "xlines": x_ms},
+            "breakdown_ms": {f: v[0] for f, v in fam.items()},
             "clocks": clk.summary()}
     if not args.no_e2e:
         line["e2e"] = e2e_measure(ctx, cfg, t, max(1, min(args.steps, 3)), world, dist)
+        t += max(1, min(args.steps, 3))
+    st = ctx.get_state()
+    ctx.close()
+    if rank == 0 and world == 1 and form == "mixed" and not args.no_plain and state2 is not None:
+        line["plain_fp64"] = plain_comparison(coefs, base, state2, t0, hbm_peak)
+        line["speedup_vs_plain"] = value / line["plain_fp64"]["value"]
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        st = ctx.get_state()
-        cpu_s = cpu_stage_sample(cfg, coefs, base, st, 1, t)
+        pcfg = workload("plain")
+        threads = os.cpu_count() or 1
+        cpu_s, used = cpu_stage_seconds(pcfg, coefs, base, st, threads, t)
         cpu_val = pts / (4.0 * cpu_s) / 1e6
-        line["cpu_baseline"] = {"value": cpu_val, "unit": "Mpt-steps/s", "cores": 1, "kind": "port",
-                                "sample": "one RK stage of the same nx=1025 ny=193 K=32 state, single thread "
-                                          "(%.1f s); per-step rate = stage rate / 4" % cpu_s}
+        line["cpu_baseline"] = {"value": cpu_val, "unit": "Mpt-steps/s", "cores": used, "kind": "port",
+                                "sample": "one RK stage of the same nx=1025 ny=193 K=32 state on %d host threads "
+                                          "(%.2f s); per-step rate = stage rate / 4" % (used, cpu_s)}
     if rank == 0:
         print(json.dumps(line), flush=True)
-
-
-def C_stream(ctx):
-    import ctypes as C
-    p = C.c_void_p()
-    ctx.lib.tb_stream(ctx.h, C.byref(p))
-    return p.value or 0
 
 
 def sor_points_per_launch(cfg):
@@ -302,14 +369,13 @@ def e2e_measure(ctx, cfg, t, steps, world, dist):
     """Steps through the C ABI with pinned host buffers copied in and out each step."""
     import torch
     shape = (cfg.kfour, cfg.ny, cfg.nx)
-    host = {n: torch.empty(shape + (2,), dtype=torch.float64, pin_memory=True)
-            for n in ("ux", "uy", "uz", "wx", "wy", "wz")}
+    host = {n: torch.empty(shape + (2,), dtype=torch.float64, pin_memory=True) for n in NAMES}
     st = ctx.get_state()
     for n, v in st.items():
         host[n].numpy()[...] = np.stack([v.real, v.imag], axis=-1)
     import ctypes as C
     D = C.POINTER(C.c_double)
-    ptrs = [C.cast(host[n].data_ptr(), D) for n in ("ux", "uy", "uz", "wx", "wy", "wz")]
+    ptrs = [C.cast(host[n].data_ptr(), D) for n in NAMES]
     nbytes = sum(h.numel() * 8 for h in host.values())
     barrier(dist)
     t0 = time.perf_counter()

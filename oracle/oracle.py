@@ -56,6 +56,8 @@ def load():
     lib.ora_rk_stage.argtypes = [P, C.c_int, C.c_int]
     lib.ora_step.argtypes = [P, C.c_int]
     lib.ora_poisson_stats.argtypes = [P, C.POINTER(C.c_int), D]
+    lib.ora_set_threads.argtypes = [C.c_int]
+    lib.ora_set_threads.restype = C.c_int
     _lib = lib
     return lib
 
@@ -189,3 +191,8 @@ class Oracle:
         r = np.zeros(K)
         self.lib.ora_poisson_stats(self.h, v, _d(r))
         return list(v), r
+
+
+def set_threads(n):
+    """Host threads of the oracle's parallel loops; returns the count in use."""
+    return int(load().ora_set_threads(int(n)))

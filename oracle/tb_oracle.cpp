@@ -6,6 +6,9 @@
 // build (oracle/Makefile) disables floating-point contraction so that the
 // arithmetic is the same on x86-64 and aarch64 hosts.
 #include "tb_oracle.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -140,9 +143,10 @@ void rhsxx_line(const C* f, C* r, int n, double dxx) {
 
 void derparx_impl(ora_ctx* o, C* ddx, const C* fc) {  // derivs_par.f:80-95
     int n = o->nx;
-    std::vector<double> gam(n); std::vector<C> u(n);
-    for (int k = 1; k <= o->K; k++)
-        for (int j = 1; j <= o->ny; j++) {
+#pragma omp parallel for schedule(static)
+    for (int q = 0; q < o->K * o->ny; q++) {
+            std::vector<double> gam(n); std::vector<C> u(n);
+            int k = 1 + q / o->ny, j = 1 + q % o->ny;
             size_t base = o->id(1, j, k);
             rhsx_line(fc + base, ddx + base, n, o->dx);
             thomas(o->a1x.data(), o->b1x.data(), o->c1x.data(), ddx + base, n, 1, gam, u);
@@ -150,9 +154,10 @@ void derparx_impl(ora_ctx* o, C* ddx, const C* fc) {  // derivs_par.f:80-95
 }
 void derparxx_impl(ora_ctx* o, C* d2, const C* fc) {  // derivs_par.f:98-113
     int n = o->nx;
-    std::vector<double> gam(n); std::vector<C> u(n);
-    for (int k = 1; k <= o->K; k++)
-        for (int j = 1; j <= o->ny; j++) {
+#pragma omp parallel for schedule(static)
+    for (int q = 0; q < o->K * o->ny; q++) {
+            std::vector<double> gam(n); std::vector<C> u(n);
+            int k = 1 + q / o->ny, j = 1 + q % o->ny;
             size_t base = o->id(1, j, k);
             rhsxx_line(fc + base, d2 + base, n, o->dxx);
             thomas(o->a2x.data(), o->b2x.data(), o->c2x.data(), d2 + base, n, 1, gam, u);
@@ -200,13 +205,14 @@ void rhsyy_line(ora_ctx* o, const C* f, C* r, size_t s) {
 void dery_impl(ora_ctx* o, C* ddy, const C* fc, int kind) {  // 0 dery, 1 deryfv, 2 deryy
     int J = o->ny;
     size_t s = o->nx;
-    std::vector<double> gam(J); std::vector<C> u(J);
     const double *a, *b, *c;
     if (kind == 0) { a = o->a1y.data(); b = o->b1y.data(); c = o->c1y.data(); }
     else if (kind == 1) { a = o->a1fv.data(); b = o->b1fv.data(); c = o->c1fv.data(); }
     else { a = o->a2y.data(); b = o->b2y.data(); c = o->c2y.data(); }
-    for (int k = 1; k <= o->K; k++)
-        for (int i = 1; i <= o->nx; i++) {
+#pragma omp parallel for schedule(static)
+    for (int q = 0; q < o->K * o->nx; q++) {
+            std::vector<double> gam(J); std::vector<C> u(J);
+            int k = 1 + q / o->nx, i = 1 + q % o->nx;
             size_t base = o->id(i, 1, k);
             if (kind == 2) rhsyy_line(o, fc + base, ddy + base, s);
             else rhsy_line(o, fc + base, ddy + base, s, kind == 1);
@@ -316,20 +322,22 @@ void p_to_f_line(int K, int P, double* dp /*1-based*/, C* cf, size_t cs) {
     cf[0] = mk(cf[0].re, 0.0);
 }
 void f_to_p_impl(ora_ctx* o, double* phys, const C* four) {  // nlterms_par.f:303
-    std::vector<double> d(o->P + 2);
     size_t n2 = (size_t)o->nx * o->ny;
+#pragma omp parallel for schedule(static)
     for (int j = 1; j <= o->ny; j++)
         for (int i = 1; i <= o->nx; i++) {
+            std::vector<double> d(o->P + 2);
             size_t p = o->id2(i, j);
             f_to_p_line(o->K, o->P, four + p, n2, d.data());
             for (int z = 1; z <= o->P; z++) phys[p + n2 * (z - 1)] = d[z];
         }
 }
 void p_to_f_impl(ora_ctx* o, C* four, double* phys) {  // nlterms_par.f:364
-    std::vector<double> d(o->P + 2);
     size_t n2 = (size_t)o->nx * o->ny;
+#pragma omp parallel for schedule(static)
     for (int j = 1; j <= o->ny; j++)
         for (int i = 1; i <= o->nx; i++) {
+            std::vector<double> d(o->P + 2);
             size_t p = o->id2(i, j);
             for (int z = 1; z <= o->P; z++) d[z] = phys[p + n2 * (z - 1)];
             p_to_f_line(o->K, o->P, d.data(), four + p, n2);
@@ -347,6 +355,7 @@ void nlterms_impl(ora_ctx* o, C* a, C* b, C* c) {
     f_to_p_impl(o, wxp.data(), o->wx.data());
     f_to_p_impl(o, wyp.data(), o->wy.data());
     f_to_p_impl(o, wzp.data(), o->wz.data());
+#pragma omp parallel for schedule(static)
     for (size_t q = 0; q < NP; q++) {
         ap[q] = uyp[q] * wxp[q] - uxp[q] * wyp[q];
         bp[q] = uxp[q] * wzp[q] - uzp[q] * wxp[q];
@@ -774,10 +783,12 @@ struct Poi {
 };
 
 void poi_uy_impl(ora_ctx* o, const C* dwzdx, double erromax) {  // poisson_par.f:6-64
-    Poi p(o);
     int msh = o->msh;
     o->pv.assign(o->K, 0); o->pres.assign(o->K, 0.0);
+    // modes are independent problems (one work set per thread)
+#pragma omp parallel for schedule(dynamic, 1)
     for (int k = 1; k <= o->K; k++) {
+        Poi p(o);
         p.function_source(dwzdx, k);
         double sum_err = 0.0;
         int vcycles, done = 0;
@@ -1501,6 +1512,17 @@ int ora_step(ora_ctx* o, int t) {
 int ora_poisson_stats(ora_ctx* o, int* v, double* r) {
     for (int k = 0; k < (int)o->pv.size(); k++) { v[k] = o->pv[k]; r[k] = o->pres[k]; }
     return (int)o->pv.size();
+}
+
+// Host threads for the parallel loops (independent lines and modes).
+int ora_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
 }
 
 }  // extern "C"

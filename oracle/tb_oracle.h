@@ -5,13 +5,15 @@
  * only the test suite, the smoke check and the CPU-baseline leg of the
  * benchmark load it.  Nothing in the product links against it.
  *
- * Pinning: the reference ships no field dumps (its base-flow files are empty
- * and it cannot be compiled without gfortran/MPI), so field-level parity is
- * pinned by (a) the reference's golden coefficient tables pre_processing/
- * coefs.bin, which feed every y-operator of this oracle, (b) the Blasius wall
- * shear of lst_ts/fpp.dat, and (c) exactness properties of each operator
- * (polynomial exactness of the compact schemes, realft round trips against a
- * plain DFT, the discrete Poisson equation satisfied to the stop tolerance).
+ * Pinning: field-level parity unpinned by reference outputs -- the reference
+ * ships no field dumps (its base-flow files are empty) and cannot be compiled
+ * here (no gfortran, no MPI).  What is pinned: (a) the reference's golden
+ * coefficient tables pre_processing/coefs.bin, which feed every y-operator of
+ * this oracle, (b) the Blasius wall shear of lst_ts/fpp.dat; the field-level
+ * routines rest on (c) exactness properties of each operator (polynomial
+ * exactness of the compact schemes, realft round trips against a plain DFT,
+ * the discrete Poisson equation satisfied to the stop tolerance) and on
+ * following the reference's loop and operation order line by line.
  *
  * Every routine follows one reference subroutine in its loop order and
  * operation order; each cites the file:line it restates.  MPI is collapsed to
@@ -65,6 +67,8 @@ int ora_rk_stage(ora_ctx* o, int stage, int t);
 int ora_step    (ora_ctx* o, int t);
 /* V-cycles and final residual of the last poi_uy, per mode. */
 int ora_poisson_stats(ora_ctx* o, int* vcycles, double* residual);
+/* Host threads of the parallel loops (n <= 0: keep); returns the count in use. */
+int ora_set_threads(int n);
 
 #ifdef __cplusplus
 }
