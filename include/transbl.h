@@ -61,6 +61,10 @@ typedef struct tb_config {
     int    ibm;         /* 1: add immersed-boundary force (cvirt)                   */
     int    precision;   /* TB_FORM_PLAIN_FP64 or TB_FORM_MIXED                      */
     int    les_damping; /* 0: reference cubic damping, 1: van Driest [1-e^{-y+/A}]^2*/
+    int    warm_start;  /* mixed form: 1 starts each stage's v-Poisson solve from the
+                           extrapolation 2 v(t-1) - v(t-2) of the same stage's solutions
+                           of the two previous steps; 0 from the current v, as the
+                           reference (no effect on the plain form)                  */
     double Re;          /* U L / nu                                    par.for:41   */
     double dx;          /* uniform x spacing                           par.for:83   */
     double dy;          /* first wall-normal spacing dy0               par.for:73   */

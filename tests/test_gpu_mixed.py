@@ -76,6 +76,14 @@ def test_poi_uy_mixed_corrections(mcase):
     assert counts[2] > 0
 
 
+def test_nlterms_mixed(mcase):
+    """Mean part exact in FP64, disturbance products through FP32 transforms:
+    the error is FP32 rounding of the quadratic disturbance term only."""
+    g, o = pair(mcase, 7)
+    for a, b in zip(g.nlterms(), o.nlterms()):
+        assert rel(a, b) < 1e-8
+
+
 def test_full_steps_mixed(mcase):
     cfg, coefs, base, ora, api = mcase
     g, o = pair(mcase, 11)

@@ -24,7 +24,7 @@ class TbConfig(C.Structure):
     """Mirror of struct tb_config (runtime replacement of par.for)."""
     _fields_ = [(n, C.c_int) for n in (
         "nx", "ny", "kfour", "kphys", "msh", "my_form", "i0", "i1", "i2", "i3", "i4", "stpp",
-        "max_vcycles", "ibm", "precision", "les_damping")] + \
+        "max_vcycles", "ibm", "precision", "les_damping", "warm_start")] + \
         [(n, C.c_double) for n in (
             "Re", "dx", "dy", "stf", "x0", "alpha", "omega", "beta", "fac_y", "alphaf", "tol_stage",
             "tol_final", "C_s", "A_plus", "irf", "ibm_xc", "ibm_zc", "ibm_h", "ibm_R")] + \

@@ -140,6 +140,7 @@ int tb_destroy(tb_ctx* c) {
                     c->ry2.w, c->ry2.off, c->ry2.cnt, c->px.lu, c->pfc, c->psc, c->pfct, c->pdef, c->pcarry,
                     c->pstate, c->perr, c->pqdy2, c->pcoef, c->wcoef};
     for (void* p : ptrs) if (p) cudaFree(p);
+    if (c->nl_phys) cudaFree(c->nl_phys);
     for (int q = 0; q < 24; q++) if (c->tmp[q]) cudaFree(c->tmp[q]);
     for (auto& r : c->prof_open) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : c->prof_pool) cudaEventDestroy(e);
@@ -182,6 +183,7 @@ int tb_init_fields(tb_ctx* c) {  // main_par.f:601-641
     if (!ready(c)) return TB_ERR_STATE;
     if (!c->have_base) { tb_set_error("base flow not set (tb_set_baseflow)"); return TB_ERR_STATE; }
     size_t n3 = tb_n3(c);
+    tb_mixed_invalidate(c);
     cplx* fields[] = {c->ux, c->uy, c->uz, c->wx, c->wy, c->wz, c->wx1, c->wy1, c->wz1, c->dv1x, c->dv1y, c->dv1z, c->dv2x, c->dv2y, c->dv2z};
     for (cplx* f : fields) TB_CUDA(cudaMemsetAsync(f, 0, n3 * sizeof(cplx), c->stream));
     TB_CUDA(cudaMemsetAsync(c->d2uydx2, 0, (size_t)c->g.nx * c->g.K * sizeof(cplx), c->stream));
@@ -234,8 +236,10 @@ int tb_rk_stage(tb_ctx* c, int stage, int t) {
     if ((r = tb_rk_update(c, stage))) return r;
     if (stage == 1 && (r = tb_ts_pert_k(c, t, 0.5))) return r;
     if (stage == 3 && (r = tb_ts_pert_k(c, t, 1.0))) return r;
+    c->ws_stage = stage; c->ws_t = t;
     if (stage < 4) r = tb_loop_impl(c, c->cfg.tol_stage, false);
     else r = tb_loop_impl(c, c->cfg.tol_final, true);
+    c->ws_stage = 0;
     if (r) return r;
     if ((r = tb_prof_end(c, PROF_STAGE, ps))) return r;
     TB_CUDA(cudaGetLastError());

@@ -114,6 +114,8 @@ struct tb_ctx {
     std::vector<cplx> hbuf;
     // mixed form
     void* mixed = nullptr;
+    int ws_stage = 0, ws_t = 0;  // RK stage and step of the running loop (0: a mirror call)
+    float* nl_phys = nullptr;    // mixed nlterms: FP32 physical disturbance of the 6 fields (6, P, nx*ny)
     // optional CUDA-event timing of kernel families (tb_profile)
     bool prof = false;
     struct ProfRec { int id; cudaEvent_t a, b; };
@@ -180,6 +182,7 @@ inline size_t tb_poi_blk_size(int ny) { return (size_t)9 * ny + 1280; }
 int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro);
 int tb_mixed_setup(tb_ctx* c);
 void tb_mixed_free(tb_ctx* c);
+void tb_mixed_invalidate(tb_ctx* c);   // forget the warm-start history (new state)
 
 // grid helpers
 inline unsigned tb_blocks(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }

@@ -67,6 +67,9 @@ struct Mixed {
     float* qdy2 = nullptr;    // (ny, msh)
     float* ainv = nullptr;    // (K, N, N) inverse of the coarsest operator per mode
     unsigned long long* maxsq = nullptr;   // (K) max |defect|^2 as double bits
+    // warm start: per RK stage the v of the last two steps' solves and their steps
+    cplx* hist[4][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+    int hist_t[4][2] = {{-9, -9}, {-9, -9}, {-9, -9}, {-9, -9}};
     int NL = 0, N = 0;
     int ptsx[MG_MAX], ptsy[MG_MAX], ylvl[MG_MAX], semi[MG_MAX], S[MG_MAX];
     double dx2[MG_MAX];
@@ -410,6 +413,20 @@ __global__ void k_direct(MgDev M) {
         ay += __shfl_xor_sync(0xffffffffu, ay, o);
     }
     if (lane == 0) M.e[(size_t)k * M.elems + M.off[l] + (size_t)n * (1 + p / m) + 1 + p % m] = f2(ax, ay);
+}
+
+// Warm start: fc = 2 h1 - h2 on the interior of the FP64 fine level (h1, h2:
+// the same stage's v of the two previous steps; the boundary rows and
+// columns keep this stage's Dirichlet data).
+__global__ void k_extrap(cplx* fc, size_t elems64, const cplx* h1, const cplx* h2, int nx, int ny, int K) {
+    size_t per = (size_t)nx * ny;
+    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * K) return;
+    int k = (int)(q / per);
+    int i = (int)((q % per) % nx), j = (int)((q % per) / nx);
+    if (i < 1 || i > nx - 2 || j < 1) return;
+    cplx a = h1[q], b = h2[q];
+    fc[(size_t)k * elems64 + (q % per)] = make_double2(2.0 * a.x - b.x, 2.0 * a.y - b.y);
 }
 
 // u += e on the interior of the FP64 fine level (fc layout: x-contiguous).
@@ -756,9 +773,18 @@ int tb_mixed_setup(tb_ctx* c) {
     return TB_OK;
 }
 
+void tb_mixed_invalidate(tb_ctx* c) {
+    Mixed* m = get(c);
+    if (!m) return;
+    for (auto& h : m->hist_t) { h[0] = -9; h[1] = -9; }
+}
+
 void tb_mixed_free(tb_ctx* c) {
     Mixed* m = get(c);
     if (!m) return;
+    for (auto& h : m->hist)
+        for (cplx* p : h)
+            if (p) cudaFree(p);
     for (void* p : {(void*)m->e, (void*)m->r, (void*)m->rr, (void*)m->tab, (void*)m->coef, (void*)m->qdy2, (void*)m->ainv,
                     (void*)m->maxsq})
         if (p) cudaFree(p);
@@ -777,6 +803,17 @@ int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
     cudaEvent_t pall = nullptr;
     if ((r = tb_prof_begin(c, PROF_POISSON, &pall))) return r;
     if ((r = tb_poisson_begin(c, dwzdx))) return r;
+    Mixed* mx = get(c);
+    const int ws = (c->cfg.warm_start && c->ws_stage >= 1 && c->ws_stage <= 4) ? c->ws_stage - 1 : -1;
+    if (ws >= 0) {
+        for (cplx*& h : mx->hist[ws])
+            if (!h) TB_CUDA(cudaMalloc(&h, tb_n3(c) * sizeof(cplx)));
+        if (mx->hist_t[ws][0] == c->ws_t - 1 && mx->hist_t[ws][1] == c->ws_t - 2) {
+            k_extrap<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(c->pfc, c->g.lvl_elems, mx->hist[ws][0],
+                                                                      mx->hist[ws][1], nx, ny, K);
+            TB_CHECK_LAUNCH(c);
+        }
+    }
     std::vector<int> hs(2 * K);
     dim3 tgrid(tb_blocks(nx, 32), tb_blocks(ny, 32), K), tblk(32, 8);
     for (int it = 0; it <= max_outer; it++) {
@@ -796,6 +833,12 @@ int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
         TB_CHECK_LAUNCH(c);
     }
     if ((r = tb_poisson_end(c))) return r;
+    if (ws >= 0) {   // keep this solve for the next steps' guesses
+        std::swap(mx->hist[ws][0], mx->hist[ws][1]);
+        TB_CUDA(cudaMemcpyAsync(mx->hist[ws][0], c->uy, tb_n3(c) * sizeof(cplx), cudaMemcpyDeviceToDevice, c->stream));
+        mx->hist_t[ws][1] = mx->hist_t[ws][0];
+        mx->hist_t[ws][0] = c->ws_t;
+    }
     if ((r = tb_prof_end(c, PROF_POISSON, pall))) return r;
     std::vector<double> he(K);
     TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));

@@ -239,7 +239,23 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor(PoiDev P, int l, int itera,
 // ---------------------------------------------------------------------------
 // The level-l operator of defect (poisson_par.f:543-793) applied to fc at the
 // interior point (i, j) of mode k: L fc = den*Dxx + q2*Dyy + k2b2*ify*M - top.
-__device__ __forceinline__ cplx poi_Lu(const PoiDev& P, int l, int k, int i, int j) {
+// The x-stencil sum of row jj (rhs_center / rhs_border incl. the diagonal):
+__device__ __forceinline__ cplx poi_bx(const PoiDev& P, int l, int k, int i, int jj) {
+    const int nxl = P.ptsx[l];
+    const cplx* F = P.fc + (size_t)k * P.elems + P.off[l] + (size_t)nxl * jj;
+    if (i == 1 || i == nxl - 2) {
+        int e = (i == 1) ? 1 : -1;
+        cplx a = F[i - e], c0 = F[i], b = F[i + e], c = F[i + 2 * e], d = F[i + 3 * e], g = F[i + 4 * e];
+        return make_double2(10.0 * a.x - 15.0 * c0.x - 4.0 * b.x + 14.0 * c.x - 6.0 * d.x + g.x,
+                            10.0 * a.y - 15.0 * c0.y - 4.0 * b.y + 14.0 * c.y - 6.0 * d.y + g.y);
+    }
+    cplx a = F[i - 2], b = F[i - 1], c0 = F[i], c = F[i + 1], d = F[i + 2];
+    return make_double2(-a.x + 16.0 * b.x - 30.0 * c0.x + 16.0 * c.x - d.x, -a.y + 16.0 * b.y - 30.0 * c0.y + 16.0 * c.y - d.y);
+}
+
+// L fc at (i, j) with the x-stencil sums supplied by bx(jj).
+template <class BX>
+__device__ __forceinline__ cplx poi_Lu_b(const PoiDev& P, int l, int k, int i, int j, BX bx) {
     const int nxl = P.ptsx[l], n = P.ptsy[l];
     const double* cf = P.coef + 24 * l;
     const double *SPc = cf, *CPc = cf + 7, *PPc = cf + 15, *LPc = cf + 19;
@@ -247,16 +263,6 @@ __device__ __forceinline__ cplx poi_Lu(const PoiDev& P, int l, int k, int i, int
     double den = P.den[l], ify = P.ify;
     const cplx* F = P.fc + (size_t)k * P.elems + P.off[l];
     auto f = [&](int ii, int jj) -> cplx { return F[(size_t)ii + (size_t)nxl * jj]; };
-    auto bx = [&](int jj) -> cplx {
-        if (i == 1 || i == nxl - 2) {
-            int e = (i == 1) ? 1 : -1;
-            cplx a = f(i - e, jj), c0 = f(i, jj), b = f(i + e, jj), c = f(i + 2 * e, jj), d = f(i + 3 * e, jj), g = f(i + 4 * e, jj);
-            return make_double2(10.0 * a.x - 15.0 * c0.x - 4.0 * b.x + 14.0 * c.x - 6.0 * d.x + g.x,
-                                10.0 * a.y - 15.0 * c0.y - 4.0 * b.y + 14.0 * c.y - 6.0 * d.y + g.y);
-        }
-        cplx a = f(i - 2, jj), b = f(i - 1, jj), c0 = f(i, jj), c = f(i + 1, jj), d = f(i + 2, jj);
-        return make_double2(-a.x + 16.0 * b.x - 30.0 * c0.x + 16.0 * c.x - d.x, -a.y + 16.0 * b.y - 30.0 * c0.y + 16.0 * c.y - d.y);
-    };
     cplx b, cc, d;
     double q2;
     double top = 0.0;
@@ -295,6 +301,10 @@ __device__ __forceinline__ cplx poi_Lu(const PoiDev& P, int l, int k, int i, int
     return make_double2(b.x * den + cc.x * q2 + d.x * ify - top * fij.x, b.y * den + cc.y * q2 + d.y * ify - top * fij.y);
 }
 
+__device__ __forceinline__ cplx poi_Lu(const PoiDev& P, int l, int k, int i, int j) {
+    return poi_Lu_b(P, l, k, i, j, [&](int jj) { return poi_bx(P, l, k, i, jj); });
+}
+
 // defect (poisson_par.f:543-793): def = sc + si * (L fc) at level l;
 // si > 0 also stores it into sc(l) (coarse right-hand side).
 __global__ void k_defect(PoiDev P, int l, double si) {
@@ -323,11 +333,20 @@ __global__ void k_defect(PoiDev P, int l, double si) {
 // defect records +inf).
 __global__ void k_defect_f32(PoiDev P, float2* r32, float2* e32, size_t elems32, unsigned long long* maxsq) {
     __shared__ float2 tile[32][33];
+    __shared__ cplx bxs[34][32];   // x-stencil sums of rows j0-1 .. j0+32, computed once
     __shared__ double wmax[8];
     const int k = blockIdx.z;
     if (!P.state[2 * k]) return;   // uniform over the block
     const int nx = P.nx, ny = P.ny;
     const int i0 = 1 + blockIdx.x * 32, j0 = 1 + blockIdx.y * 32;
+    {
+        const int i = i0 + threadIdx.x;
+        for (int r = threadIdx.y; r < 34; r += 8) {
+            int jj = j0 - 1 + r;
+            bxs[r][threadIdx.x] = (i <= nx - 2 && jj >= 1 && jj <= ny - 1) ? poi_bx(P, 0, k, i, jj) : make_double2(0.0, 0.0);
+        }
+    }
+    __syncthreads();
     double m = 0.0;
     bool bad = false;
     for (int r = threadIdx.y; r < 32; r += 8) {
@@ -335,7 +354,7 @@ __global__ void k_defect_f32(PoiDev P, float2* r32, float2* e32, size_t elems32,
         float2 v32 = make_float2(0.f, 0.f);
         if (i <= nx - 2 && j <= ny - 1) {
             cplx s = P.sc[(size_t)k * P.elems + (size_t)i + (size_t)nx * j];
-            cplx Lu = poi_Lu(P, 0, k, i, j);
+            cplx Lu = poi_Lu_b(P, 0, k, i, j, [&](int jj) { return bxs[jj - j0 + 1][threadIdx.x]; });
             cplx v = make_double2(s.x - Lu.x, s.y - Lu.y);
             double a = v.x * v.x + v.y * v.y;
             if (!(a <= 1.7e308)) bad = true;

@@ -15,11 +15,18 @@
 
 #define TW_N 512
 __constant__ double c_twr[TW_N], c_twi[TW_N];  // e^{-2 pi i t / TW_N}
+__constant__ float c_twrf[TW_N], c_twif[TW_N]; // the same, rounded to FP32
 
 namespace {
 
 __device__ __forceinline__ double twr(int t) { return c_twr[t & (TW_N - 1)]; }
 __device__ __forceinline__ double twi(int t) { return c_twi[t & (TW_N - 1)]; }
+template <class R> __device__ __forceinline__ R tw_r(int t);
+template <class R> __device__ __forceinline__ R tw_i(int t);
+template <> __device__ __forceinline__ double tw_r<double>(int t) { return c_twr[t & (TW_N - 1)]; }
+template <> __device__ __forceinline__ double tw_i<double>(int t) { return c_twi[t & (TW_N - 1)]; }
+template <> __device__ __forceinline__ float tw_r<float>(int t) { return c_twrf[t & (TW_N - 1)]; }
+template <> __device__ __forceinline__ float tw_i<float>(int t) { return c_twif[t & (TW_N - 1)]; }
 
 template <int N>
 __device__ __forceinline__ int brev(int i) {
@@ -31,13 +38,13 @@ __device__ __forceinline__ int brev(int i) {
 
 // In-place radix-2 complex FFT of length N. SIGN = -1: sum X_k e^{-2 pi i km/N};
 // SIGN = +1: sum X_k e^{+2 pi i km/N}.
-template <int N, int SIGN>
-__device__ __forceinline__ void cfft(double* re, double* im) {
+template <int N, int SIGN, class R = double>
+__device__ __forceinline__ void cfft(R* re, R* im) {
 #pragma unroll
     for (int i = 0; i < N; i++) {
         int j = brev<N>(i);
         if (j > i) {
-            double t = re[i]; re[i] = re[j]; re[j] = t;
+            R t = re[i]; re[i] = re[j]; re[j] = t;
             t = im[i]; im[i] = im[j]; im[j] = t;
         }
     }
@@ -49,15 +56,15 @@ __device__ __forceinline__ void cfft(double* re, double* im) {
 #pragma unroll
             for (int q = 0; q < h; q++) {
                 int a = s + q, b = a + h;
-                double tr, ti;
+                R tr, ti;
                 if (q == 0) {
                     tr = re[b]; ti = im[b];
                 } else if (4 * q == len) {  // twiddle -SIGN*i ... e^{SIGN*i*pi/2} = SIGN*i
                     tr = (SIGN < 0) ? im[b] : -im[b];
                     ti = (SIGN < 0) ? -re[b] : re[b];
                 } else {
-                    double wr = twr(q * (TW_N / len));
-                    double wi = (SIGN < 0) ? twi(q * (TW_N / len)) : -twi(q * (TW_N / len));
+                    R wr = tw_r<R>(q * (TW_N / len));
+                    R wi = (SIGN < 0) ? tw_i<R>(q * (TW_N / len)) : -tw_i<R>(q * (TW_N / len));
                     tr = wr * re[b] - wi * im[b];
                     ti = wr * im[b] + wi * re[b];
                 }
@@ -165,6 +172,121 @@ __global__ void __launch_bounds__(128) k_nlterms(NlArgs A) {
     to_four<P>(ph[0], A.K, A.a + q, cs);
     to_four<P>(ph[1], A.K, A.b + q, cs);
     to_four<P>(ph[2], A.K, A.c + q, cs);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed form of nlterms_fi.  With every field split into its spanwise mean
+// M = Re c_0 (which carries the base flow) and its z-varying part d(z), a
+// product such as uy wx transforms to
+//   mode 0:   M_uy M_wx                 + T(d_uy d_wx)_0
+//   mode k:   M_uy wx_k + M_wx uy_k     + T(d_uy d_wx)_k      (k >= 1)
+// because T(M d)_k = M c_k(d) exactly (T the forward transform of the
+// reference; d holds modes 1..K-1 and the packed Nyquist term).  The linear
+// part, which dominates for a disturbance on a base flow, stays in FP64;
+// only the quadratic disturbance term goes through FP32 transforms.
+// Components below 1e-14 are zeroed and Im c_0 = 0, as nlterms_par.f does.
+
+// z-varying part of a field (mean removed) -> physical p[0..P-1], FP32.
+template <int P>
+__device__ __forceinline__ void to_phys_dist(const cplx* __restrict__ cf, size_t cs, int K, float* p) {
+    constexpr int N = P / 2;
+    float re[N], im[N];
+    float CN = (float)(0.5 * cf[0].y);
+    re[0] = CN; im[0] = -CN;
+#pragma unroll
+    for (int k = 1; k < N; k++) {
+        cplx A = (k < K) ? cf[(size_t)k * cs] : make_double2(0.0, 0.0);
+        cplx Bc = (N - k < K) ? cf[(size_t)(N - k) * cs] : make_double2(0.0, 0.0);
+        float Ar = (float)A.x, Ai = (float)A.y, Br = (float)Bc.x, Bi = -(float)Bc.y;
+        float sr = 0.5f * (Ar + Br), si = 0.5f * (Ai + Bi);
+        float dr = 0.5f * (Ar - Br), di = 0.5f * (Ai - Bi);
+        float wr = tw_r<float>(k * (TW_N / P)), wi = tw_i<float>(k * (TW_N / P));
+        re[k] = sr - (wr * di + wi * dr);
+        im[k] = si + (wr * dr - wi * di);
+    }
+    cfft<N, -1, float>(re, im);
+#pragma unroll
+    for (int m = 0; m < N; m++) { p[2 * m] = re[m]; p[2 * m + 1] = im[m]; }
+}
+
+// physical p[0..P-1] -> modes 0..N-1 in FP32 (re[k], im[k]; Im c_0 = 0).
+template <int P>
+__device__ __forceinline__ void to_four_f(const float* p, float* cr, float* ci) {
+    constexpr int N = P / 2;
+    float re[N], im[N];
+#pragma unroll
+    for (int m = 0; m < N; m++) { re[m] = p[2 * m]; im[m] = p[2 * m + 1]; }
+    cfft<N, +1, float>(re, im);
+    const float invP = 1.0f / (float)P, two_P = 2.0f / (float)P;
+    cr[0] = (re[0] + im[0]) * invP; ci[0] = 0.0f;
+#pragma unroll
+    for (int k = 1; k < N; k++) {
+        float Fr = re[k], Fi = im[k], Gr = re[N - k], Gi = -im[N - k];
+        float Er = 0.5f * (Fr + Gr), Ei = 0.5f * (Fi + Gi);
+        float gr = Fr - Gr, gi = Fi - Gi;
+        float Or = 0.5f * gi, Oi = -0.5f * gr;
+        float vr = tw_r<float>(k * (TW_N / P)), vi = -tw_i<float>(k * (TW_N / P));
+        cr[k] = two_P * (Er + (vr * Or - vi * Oi));
+        ci[k] = two_P * (Ei + (vr * Oi + vi * Or));
+    }
+}
+
+// Pass 1: one thread per (field f, point q): the FP32 physical disturbance
+// d_f(z) into ph[(f * P + z) * n2 + q].
+template <int P>
+__global__ void __launch_bounds__(128) k_nl_phys(NlArgs A, float* __restrict__ ph) {
+    const size_t n2 = A.n2;
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= 6 * n2) return;
+    const int f = (int)(t / n2);
+    const size_t q = t - (size_t)f * n2;
+    const cplx* F = (f == 0) ? A.ux : (f == 1) ? A.uy : (f == 2) ? A.uz : (f == 3) ? A.wx : (f == 4) ? A.wy : A.wz;
+    float p[P];
+    to_phys_dist<P>(F + q, n2, A.K, p);
+    float* o = ph + (size_t)f * P * n2 + q;
+#pragma unroll
+    for (int z = 0; z < P; z++) o[(size_t)z * n2] = p[z];
+}
+
+// Pass 2: one thread per (output o, point q): the quadratic disturbance term
+// through the FP32 forward transform, plus the FP64 mean terms.
+// out = f[p1] f[q1] - f[p2] f[q2]: a = uy wx - ux wy, b = ux wz - uz wx, c = uz wy - uy wz.
+template <int P>
+__global__ void __launch_bounds__(128) k_nl_four(NlArgs A, const float* __restrict__ ph) {
+    constexpr int N = P / 2;
+    const size_t n2 = A.n2;
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= 3 * n2) return;
+    const int o = (int)(t / n2);
+    const size_t q = t - (size_t)o * n2;
+    const int p1 = (o == 0) ? 1 : (o == 1) ? 0 : 2, q1 = (o == 0) ? 3 : (o == 1) ? 5 : 4;
+    const int p2 = (o == 0) ? 0 : (o == 1) ? 2 : 1, q2 = (o == 0) ? 4 : (o == 1) ? 3 : 5;
+    const float *a1 = ph + (size_t)p1 * P * n2 + q, *b1 = ph + (size_t)q1 * P * n2 + q;
+    const float *a2 = ph + (size_t)p2 * P * n2 + q, *b2 = ph + (size_t)q2 * P * n2 + q;
+    float p[P];
+#pragma unroll
+    for (int z = 0; z < P; z++) {
+        size_t zz = (size_t)z * n2;
+        p[z] = a1[zz] * b1[zz] - a2[zz] * b2[zz];
+    }
+    float cr[N], ci[N];
+    to_four_f<P>(p, cr, ci);
+    auto fld = [&](int f) -> const cplx* {
+        return (f == 0) ? A.ux : (f == 1) ? A.uy : (f == 2) ? A.uz : (f == 3) ? A.wx : (f == 4) ? A.wy : A.wz;
+    };
+    const cplx *P1 = fld(p1) + q, *Q1 = fld(q1) + q, *P2 = fld(p2) + q, *Q2 = fld(q2) + q;
+    const double m1 = P1[0].x, n1 = Q1[0].x, m2 = P2[0].x, n2v = Q2[0].x;
+    cplx* out = ((o == 0) ? A.a : (o == 1) ? A.b : A.c) + q;
+    out[0] = make_double2(zap(m1 * n1 - m2 * n2v + (double)cr[0]), 0.0);
+#pragma unroll
+    for (int k = 1; k < N; k++) {
+        if (k >= A.K) continue;
+        size_t kk = (size_t)k * n2;
+        cplx aq1 = Q1[kk], ap1 = P1[kk], aq2 = Q2[kk], ap2 = P2[kk];
+        double vr = m1 * aq1.x + n1 * ap1.x - m2 * aq2.x - n2v * ap2.x + (double)cr[k];
+        double vi = m1 * aq1.y + n1 * ap1.y - m2 * aq2.y - n2v * ap2.y + (double)ci[k];
+        out[kk] = make_double2(zap(vr), zap(vi));
+    }
 }
 
 // Smagorinsky eddy viscosity and force nu_t lap(u) (les_par.f:6-211).
@@ -330,6 +452,10 @@ int ensure_twiddles(tb_ctx* c) {
     }
     TB_CUDA(cudaMemcpyToSymbol(c_twr, hr, sizeof hr));
     TB_CUDA(cudaMemcpyToSymbol(c_twi, hi, sizeof hi));
+    float fr[TW_N], fi[TW_N];
+    for (int t = 0; t < TW_N; t++) { fr[t] = (float)hr[t]; fi[t] = (float)hi[t]; }
+    TB_CUDA(cudaMemcpyToSymbol(c_twrf, fr, sizeof fr));
+    TB_CUDA(cudaMemcpyToSymbol(c_twif, fi, sizeof fi));
     if (dev >= 0 && dev < 64) g_tw_ready[dev] = true;
     return TB_OK;
 }
@@ -370,10 +496,18 @@ int tb_launch_nlterms(tb_ctx* c, cplx* a, cplx* b, cplx* cc) {
     int r = ensure_twiddles(c);
     if (r) return r;
     NlArgs A{c->ux, c->uy, c->uz, c->wx, c->wy, c->wz, a, b, cc, (int)tb_n2(c), c->g.K};
-    unsigned nb = tb_blocks(A.n2, 128);
     cudaEvent_t ps = nullptr;
     if ((r = tb_prof_begin(c, PROF_NLTERMS, &ps))) return r;
-    TB_DISPATCH_P(c->g.P, (k_nlterms<PP><<<nb, 128, 0, c->stream>>>(A)));
+    if (c->cfg.precision == TB_FORM_MIXED && c->g.P >= 4) {
+        size_t need = (size_t)6 * c->g.P * A.n2;
+        if (!c->nl_phys) TB_CUDA(cudaMalloc(&c->nl_phys, need * sizeof(float)));
+        TB_DISPATCH_P(c->g.P, (k_nl_phys<PP><<<tb_blocks(6 * (size_t)A.n2, 128), 128, 0, c->stream>>>(A, c->nl_phys)));
+        TB_CHECK_LAUNCH(c);
+        TB_DISPATCH_P(c->g.P, (k_nl_four<PP><<<tb_blocks(3 * (size_t)A.n2, 128), 128, 0, c->stream>>>(A, c->nl_phys)));
+    } else {
+        unsigned nb = tb_blocks(A.n2, 128);
+        TB_DISPATCH_P(c->g.P, (k_nlterms<PP><<<nb, 128, 0, c->stream>>>(A)));
+    }
     TB_CHECK_LAUNCH(c);
     return tb_prof_end(c, PROF_NLTERMS, ps);
 }
