@@ -176,6 +176,20 @@ int tb_cvirt   (tb_ctx* ctx, double* fx, double* fy, double* fz);  /* immersed_p
 int tb_f_to_p  (tb_ctx* ctx, double* phys, const double* four);
 int tb_p_to_f  (tb_ctx* ctx, double* four, const double* phys);
 
+/* ---- on-disk formats of the reference (escreve_par.f) ------------------ */
+/* data_XX.bin checkpoint, gfortran sequential unformatted: record 1 integer*4
+   t, record 2 ux,uy,uz,wx,wy,wz (escreve, escreve_par.f:6-31) -- the file the
+   Fortran host writes and reads back at restart (main_par.f:762-769). */
+int tb_write_checkpoint(tb_ctx* ctx, const char* path, int t);
+int tb_read_checkpoint(tb_ctx* ctx, const char* path, int* t);
+/* pert_XX_YY snapshot of escreve2 (escreve_par.f:34-81): one record with ux,
+   the base flow removed from the real part of mode 0 in form 0. */
+int tb_write_pert(tb_ctx* ctx, const char* path);
+/* Largest subrecord written (default 2^31 - 9 bytes, as gfortran); records
+   beyond it are split with negated markers.  A small value exercises the
+   layout of records over 2 GiB on small files. */
+int tb_io_set_subrecord_limit(long long bytes);
+
 /* ---- device-resident access (no host copies) ------------------------- */
 /* Device pointers of the resident fields: which = 0..5 for ux,uy,uz,wx,wy,wz. */
 int tb_device_field(tb_ctx* ctx, int which, void** dptr);

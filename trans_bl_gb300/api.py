@@ -101,6 +101,10 @@ def load():
     lib.tb_filter_trid_noalloc.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, C.c_double, P]
     lib.tb_profile.argtypes = [P, C.c_int]
     lib.tb_profile_read.argtypes = [P, C.c_int, D, C.POINTER(C.c_longlong)]
+    lib.tb_write_checkpoint.argtypes = [P, C.c_char_p, C.c_int]
+    lib.tb_read_checkpoint.argtypes = [P, C.c_char_p, C.POINTER(C.c_int)]
+    lib.tb_write_pert.argtypes = [P, C.c_char_p]
+    lib.tb_io_set_subrecord_limit.argtypes = [C.c_longlong]
     _lib = lib
     return lib
 
@@ -256,6 +260,18 @@ class Context:
 
     PROF = {"sor": 0, "poi_uy": 1, "nlterms": 2, "xlines": 3, "ylines": 4, "stage": 5, "penta": 6, "defect": 7,
             "relax0": 8}
+
+    # on-disk formats of the reference (escreve_par.f)
+    def write_checkpoint(self, path, t):
+        self._c(self.lib.tb_write_checkpoint(self.h, os.fsencode(path), int(t)), "tb_write_checkpoint")
+
+    def read_checkpoint(self, path):
+        t = C.c_int(0)
+        self._c(self.lib.tb_read_checkpoint(self.h, os.fsencode(path), C.byref(t)), "tb_read_checkpoint")
+        return t.value
+
+    def write_pert(self, path):
+        self._c(self.lib.tb_write_pert(self.h, os.fsencode(path)), "tb_write_pert")
 
     def profile(self, enable):
         self._c(self.lib.tb_profile(self.h, 1 if enable else 0), "tb_profile")

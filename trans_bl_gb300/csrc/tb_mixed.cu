@@ -126,12 +126,21 @@ __global__ void __launch_bounds__(RELAX_THREADS) k_relax(MgDev M, int l, int fir
     float2* rs = g + n;
     float2* E = M.e + (size_t)k * M.elems + M.off[l];
     const float2* R = M.r + (size_t)k * M.elems + M.off[l] + (size_t)n * i;
-    for (int j = lane; j < n; j += 32) g[j] = xsum(E, n, i, j, type, dir);
+    // rows j = lane + 32 q, q < S (32 S >= n): all loads of the line issue at once
+    float2 rv[S];
+#pragma unroll
+    for (int q = 0; q < S; q++) {
+        int j = lane + 32 * q;
+        if (j < n) { g[j] = xsum(E, n, i, j, type, dir); rv[q] = R[j]; }
+    }
     __syncwarp();
     const float* cf = M.coef + 24 * M.ylvl[l];
     const float sp2 = cf[1], sp3 = cf[2], cp1 = cf[7], cp2 = cf[8], cp3 = cf[9];
     const float qx = M.qx[l];
-    for (int j = lane; j < n; j += 32) {
+#pragma unroll
+    for (int q = 0; q < S; q++) {
+        int j = lane + 32 * q;
+        if (j >= n) break;
         float2 v = f2(0.f, 0.f);
         if (j >= 1) {
             float2 t;
@@ -139,7 +148,7 @@ __global__ void __launch_bounds__(RELAX_THREADS) k_relax(MgDev M, int l, int fir
             else if (j <= n - 3)
                 t = f2(cp1 * g[j - 1].x + cp2 * g[j].x + cp3 * g[j + 1].x, cp1 * g[j - 1].y + cp2 * g[j].y + cp3 * g[j + 1].y);
             else t = g[j];
-            float2 s = R[j];
+            float2 s = rv[q];
             v = f2(s.x - qx * t.x, s.y - qx * t.y);
         }
         rs[j] = v;
@@ -219,8 +228,11 @@ __global__ void __launch_bounds__(RELAX_THREADS) k_relax(MgDev M, int l, int fir
     }
     __syncwarp();
     float2* Ei = E + (size_t)n * i;
-    for (int j = lane; j < n; j += 32)
-        if (j >= 1) Ei[j] = rs[j];
+#pragma unroll
+    for (int q = 0; q < S; q++) {
+        int j = lane + 32 * q;
+        if (j >= 1 && j < n) Ei[j] = rs[j];
+    }
 }
 
 // FP32 residual rr = r - L e at level l (interior columns, rows >= 1):
