@@ -124,6 +124,27 @@ int tb_fs_wall_shear(double beta_fs, double* fpp);
 /* Base flow on the (nx, ny) grid (fs_sch.f90:58-162), column-major reals. */
 int tb_baseflow_fs(const tb_config* cfg, double beta_fs, double* uxb, double* uyb, double* wzb);
 
+/* ---- linear stability theory for the TS-wave check (lst_ts/ose_bl.f) ---- */
+/* Spatial Orr-Sommerfeld/Squire stability of the Falkner-Skan layer: the
+   reference's continuation from a starting eigenvalue to the target
+   parameters (steps per parameter: 1000 in the reference), then the march
+   over stations x = 1 + (i-1) dx with Re^(1/2) = re_dns sqrt(x), scaled
+   frequency w0 = omega_dns Re^(1/2)/re_dns and beta scaled the same way. */
+typedef struct tb_lst_config {
+    double re0, w0, alfa0_re, alfa0_im;   /* starting point and eigenvalue guess (ose3d.in)  */
+    int    jedge;                         /* wall-normal points of the mapped grid           */
+    double bl, etamax, beta, wslope;      /* integration fraction, eta_max, beta, f''(0)     */
+    double re_dns, omega_dns, beta_dns;   /* target Re^(1/2), w/Re^(1/2), beta/Re^(1/2) (datalst.dat) */
+    int    imax;                          /* stations                                        */
+    double dx;                            /* station spacing in x / x0                       */
+    int    steps;                         /* continuation steps per parameter                */
+} tb_lst_config;
+/* Outputs per station i: x, Re^(1/2), scaled frequency and the eigenvalue
+   alpha0 = (alpha[2i], alpha[2i+1]); the growth rate is -Im(alpha0).
+   fpp, betafs: wall shear f''(0) and Falkner-Skan beta per station. */
+int tb_lst_march(const tb_lst_config* cfg, const double* fpp, const double* betafs, double* x,
+                 double* re0, double* w0, double* alpha);
+
 /* ---- lifecycle --------------------------------------------------------- */
 int tb_create(const tb_config* cfg, tb_ctx** out);
 int tb_destroy(tb_ctx* ctx);

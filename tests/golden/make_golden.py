@@ -11,7 +11,11 @@ It reads (never modifies) these data files of the reference:
                                penultimate Poisson weights are 2/(1+s), -2/s, 2/(s(1+s)))
   lst_ts/fpp.dat            -- Blasius wall shear per station (main_fs.f90:24-29)
   lst_ts/lst.dat            -- LST growth rate along x (lst_ts/ose_bl.f:81-98)
-and writes coefs_stf1.01_lvl4.json, fpp.json and lst.json beside this script.
+  lst_ts/saida              -- LST station log: x, Re^(1/2), scaled frequency and
+                               the eigenvalue alpha0 per station (ose_bl.f:91)
+  lst_ts/ose3d.in           -- the LST starting point (namelist osedata)
+and writes coefs_stf1.01_lvl4.json, fpp.json, lst.json and lst_saida.json
+beside this script.
 """
 import json
 import os
@@ -58,6 +62,19 @@ def main(ref):
     dl = open(os.path.join(ref, "lst_ts", "datalst.dat")).read().split()
     json.dump({"source": "lst_ts/lst.dat", "datalst": dl, "x": xs, "minus_alpha_i_scaled": al},
               open(os.path.join(here, "lst.json"), "w"))
+    import re
+    num = re.compile(r"[-+]?\d*\.\d+(?:[EeDd][-+]?\d+)?")
+    rows = [[float(t.replace("D", "E")) for t in num.findall(l)] for l in open(os.path.join(ref, "lst_ts", "saida"))]
+    rows = [r for r in rows if len(r) == 5]
+    keep = list(range(0, len(rows), 4)) + ([len(rows) - 1] if (len(rows) - 1) % 4 else [])
+    nml = {}
+    for line in open(os.path.join(ref, "lst_ts", "ose3d.in")):
+        if "=" in line:
+            k, v = line.split("=", 1)
+            nml[k.strip()] = v.strip().rstrip(",")
+    json.dump({"source": "lst_ts/saida, lst_ts/ose3d.in", "stations": len(rows), "dx": rows[1][0] - rows[0][0],
+               "osedata": nml, "index": keep, "rows_x_re0_w0_alpha_re_alpha_im": [rows[i] for i in keep]},
+              open(os.path.join(here, "lst_saida.json"), "w"))
     print("wrote fixtures to", here)
 
 

@@ -44,6 +44,13 @@ class PoissonStats(C.Structure):
                 ("solves", C.c_int), ("noconv", C.c_int)]
 
 
+class LstConfig(C.Structure):
+    """struct tb_lst_config (include/transbl.h)."""
+    _fields_ = [(n, C.c_double) for n in ("re0", "w0", "alfa0_re", "alfa0_im")] + [("jedge", C.c_int)] + \
+        [(n, C.c_double) for n in ("bl", "etamax", "beta", "wslope", "re_dns", "omega_dns", "beta_dns")] + \
+        [("imax", C.c_int), ("dx", C.c_double), ("steps", C.c_int)]
+
+
 class TbError(RuntimeError):
     pass
 
@@ -101,6 +108,7 @@ def load():
     lib.tb_filter_trid_noalloc.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, C.c_double, P]
     lib.tb_profile.argtypes = [P, C.c_int]
     lib.tb_profile_read.argtypes = [P, C.c_int, D, C.POINTER(C.c_longlong)]
+    lib.tb_lst_march.argtypes = [C.POINTER(LstConfig), D, D, D, D, D, D]
     lib.tb_write_checkpoint.argtypes = [P, C.c_char_p, C.c_int]
     lib.tb_read_checkpoint.argtypes = [P, C.c_char_p, C.POINTER(C.c_int)]
     lib.tb_write_pert.argtypes = [P, C.c_char_p]
@@ -351,3 +359,20 @@ class Context:
         out = self.field()
         self._c(self.lib.tb_p_to_f(self.h, dptr(out.view(np.float64)), dptr(phys)), "tb_p_to_f")
         return out
+
+
+def lst_march(re0, w0, alfa0, re_dns, omega_dns, beta_dns, imax, dx, fpp, betafs=None, jedge=251, bl=0.7,
+              etamax=7.0, beta=0.0, wslope=0.3320548, steps=1000):
+    """Spatial LST of the Falkner-Skan layer (tb_lst_march): continuation from
+    (re0, w0, alfa0) to the target, then the station march; returns x, Re^(1/2),
+    scaled frequency and the complex eigenvalue alpha0 per station."""
+    cfg = LstConfig(re0=re0, w0=w0, alfa0_re=alfa0.real, alfa0_im=alfa0.imag, jedge=jedge, bl=bl, etamax=etamax,
+                    beta=beta, wslope=wslope, re_dns=re_dns, omega_dns=omega_dns, beta_dns=beta_dns, imax=imax,
+                    dx=dx, steps=steps)
+    fpp = np.ascontiguousarray(np.broadcast_to(np.asarray(fpp, dtype=np.float64), (imax,)))
+    betafs = np.zeros(imax) if betafs is None else np.ascontiguousarray(np.broadcast_to(
+        np.asarray(betafs, dtype=np.float64), (imax,)))
+    x, r, w = np.zeros(imax), np.zeros(imax), np.zeros(imax)
+    a = np.zeros(2 * imax)
+    check(load().tb_lst_march(C.byref(cfg), dptr(fpp), dptr(betafs), dptr(x), dptr(r), dptr(w), dptr(a)), "tb_lst_march")
+    return {"x": x, "re0": r, "w0": w, "alpha": a[0::2] + 1j * a[1::2]}
