@@ -59,8 +59,8 @@ def dist_init():
     if world > 1:
         import torch
         import torch.distributed as dist
-        local = int(os.environ.get("LOCAL_RANK", "0"))
-        torch.cuda.set_device(local)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         return rank, world, dist
     return rank, world, None
@@ -75,9 +75,16 @@ def max_over_ranks(dist, v):
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_rate(world, pts, steps, seconds_max):
+    """Whole-job Mpt-steps/s of `world` independent replicas, each advancing
+    `pts` points by `steps` steps, over the slowest replica's time."""
+    return world * pts * steps / seconds_max / 1e6
 
 
 class Clocks:
@@ -301,7 +308,7 @@ def main():
     ctx.profile(False)
     ms_max = max_over_ranks(dist, ms)
     ms_per_step = ms_max / args.steps
-    value = world * pts * args.steps / (ms_max * 1e-3) / 1e6
+    value = job_rate(world, pts, args.steps, ms_max * 1e-3)
     hbm_peak, peak_kind = peaks()
     stats = ctx.poisson_stats()
     if form == "plain":
@@ -397,7 +404,7 @@ def e2e_measure(ctx, cfg, t, steps, world, dist):
     el = time.perf_counter() - t0
     el = max_over_ranks(dist, el)
     pts = cfg.nx * cfg.ny * cfg.kfour
-    return {"value": world * pts * steps / el / 1e6, "unit": "Mpt-steps/s", "h2d_bytes_per_step": nbytes,
+    return {"value": job_rate(world, pts, steps, el), "unit": "Mpt-steps/s", "h2d_bytes_per_step": nbytes,
             "d2h_bytes_per_step": nbytes, "steps": steps}
 
 
