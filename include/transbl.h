@@ -65,6 +65,11 @@ typedef struct tb_config {
                            extrapolation 2 v(t-1) - v(t-2) of the same stage's solutions
                            of the two previous steps; 0 from the current v, as the
                            reference (no effect on the plain form)                  */
+    int    step_graph;  /* mixed form: 1 runs tb_step/tb_steps as a recorded CUDA graph,
+                           each Poisson correction loop a device-side WHILE loop, so a
+                           step has no host synchronisation inside; 0 launches every
+                           kernel from the host.  tb_rk_stage and profiling always
+                           launch from the host.                                    */
     double Re;          /* U L / nu                                    par.for:41   */
     double dx;          /* uniform x spacing                           par.for:83   */
     double dy;          /* first wall-normal spacing dy0               par.for:73   */
@@ -167,6 +172,17 @@ int tb_rk_stage(tb_ctx* ctx, int stage, int t);   /* stage 1..4 of step t       
 int tb_step(tb_ctx* ctx, int t);                  /* four stages                 */
 int tb_steps(tb_ctx* ctx, int t0, int nsteps);    /* t0 .. t0+nsteps-1           */
 int tb_get_poisson_stats(tb_ctx* ctx, tb_poisson_stats* st);
+
+/* ---- ensembles: independent runs advanced together --------------------
+   One recorded CUDA graph advances every member by one step: the members'
+   stages run concurrently on the device and the host waits once per step.
+   Members use the mixed form and may differ in every size and parameter;
+   between ensemble steps each stays usable on its own.  An ensemble holds
+   its members' device buffers: destroy it before any member.             */
+typedef struct tb_ensemble tb_ensemble;
+int tb_ensemble_create(tb_ctx* const* members, int n, tb_ensemble** out);
+int tb_ensemble_step(tb_ensemble* ens, const int* t);   /* t[i]: step of member i */
+int tb_ensemble_destroy(tb_ensemble* ens);
 
 /* ---- per-subroutine mirrors (host pointers, copy in / out) ------------ */
 int tb_derparx (tb_ctx* ctx, double* ddx,   const double* fc);  /* derivs_par.f:80  */

@@ -24,7 +24,7 @@ class TbConfig(C.Structure):
     """Mirror of struct tb_config (runtime replacement of par.for)."""
     _fields_ = [(n, C.c_int) for n in (
         "nx", "ny", "kfour", "kphys", "msh", "my_form", "i0", "i1", "i2", "i3", "i4", "stpp",
-        "max_vcycles", "ibm", "precision", "les_damping", "warm_start")] + \
+        "max_vcycles", "ibm", "precision", "les_damping", "warm_start", "step_graph")] + \
         [(n, C.c_double) for n in (
             "Re", "dx", "dy", "stf", "x0", "alpha", "omega", "beta", "fac_y", "alphaf", "tol_stage",
             "tol_final", "C_s", "A_plus", "irf", "ibm_xc", "ibm_zc", "ibm_h", "ibm_R")] + \
@@ -113,6 +113,9 @@ def load():
     lib.tb_read_checkpoint.argtypes = [P, C.c_char_p, C.POINTER(C.c_int)]
     lib.tb_write_pert.argtypes = [P, C.c_char_p]
     lib.tb_io_set_subrecord_limit.argtypes = [C.c_longlong]
+    lib.tb_ensemble_create.argtypes = [C.POINTER(P), C.c_int, C.POINTER(P)]
+    lib.tb_ensemble_step.argtypes = [P, C.POINTER(C.c_int)]
+    lib.tb_ensemble_destroy.argtypes = [P]
     _lib = lib
     return lib
 
@@ -376,3 +379,36 @@ def lst_march(re0, w0, alfa0, re_dns, omega_dns, beta_dns, imax, dx, fpp, betafs
     a = np.zeros(2 * imax)
     check(load().tb_lst_march(C.byref(cfg), dptr(fpp), dptr(betafs), dptr(x), dptr(r), dptr(w), dptr(a)), "tb_lst_march")
     return {"x": x, "re0": r, "w0": w, "alpha": a[0::2] + 1j * a[1::2]}
+
+
+class Ensemble:
+    """Independent runs (mixed-form Contexts of any sizes) advanced together:
+    one recorded CUDA graph per step holds every member's four stages
+    (tb_ensemble_*).  The members stay usable on their own between steps;
+    close the ensemble before them."""
+
+    def __init__(self, members):
+        self.lib = load()
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.h.value if hasattr(m.h, "value") else m.h for m in self.members])
+        h = C.c_void_p()
+        check(self.lib.tb_ensemble_create(arr, len(self.members), C.byref(h)), "tb_ensemble_create")
+        self.h = h
+
+    def step(self, t):
+        """Advance member i by its step t[i] (an int applies to every member)."""
+        if isinstance(t, int):
+            t = [t] * len(self.members)
+        ts = (C.c_int * len(self.members))(*[int(v) for v in t])
+        check(self.lib.tb_ensemble_step(self.h, ts), "tb_ensemble_step")
+
+    def close(self):
+        if self.h:
+            self.lib.tb_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

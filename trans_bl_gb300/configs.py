@@ -71,6 +71,41 @@ def config2(**kw):
     return blasius_ts_config(1025, 193, 32, 64, 4, **kw)
 
 
+def stable_steps_per_period(cfg, limit=1.3):
+    """Smallest power of two (>= 256) of steps per forcing period keeping the
+    explicit RK4 viscous term at nu dt lambda_max <= limit, lambda_max =
+    6.86 / dy0^2 (stability bound 2.78)."""
+    period = 2.0 * math.pi / cfg.omega
+    need = period * 6.86 / (cfg.Re * cfg.fac_y * cfg.dy ** 2 * limit)
+    n = 256
+    while n < need:
+        n *= 2
+    return n
+
+
+def config3(seed=20261203, members=12, **kw):
+    """Ensemble of independent runs of uneven sizes: nx in {257, 513, 769,
+    1025}, ny in {97, 129, 193}, kfour in {8, 16, 32} (P = 2 kfour),
+    F ~ U[0.6e-4, 1.4e-4], 2D TS amplitude ~ log-U[1e-6, 1e-4] with an
+    oblique pair at a tenth of it; each member at the steps per period its
+    first cell needs.  Drawn from numpy's PCG64 seeded with `seed`."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for m in range(members):
+        nx = int(rng.choice([257, 513, 769, 1025]))
+        ny = int(rng.choice([97, 129, 193]))
+        K = int(rng.choice([8, 16, 32]))
+        F = float(rng.uniform(0.6e-4, 1.4e-4))
+        A = float(math.exp(rng.uniform(math.log(1e-6), math.log(1e-4))))
+        args = dict(F=F, amp2d=A, amp3d=0.1 * A, seed=seed + 1 + m)
+        args.update(kw)
+        cfg = blasius_ts_config(nx, ny, K, 2 * K, 4, **args)
+        if "steps_per_period" not in kw:
+            cfg.stpp = stable_steps_per_period(cfg)
+        out.append(cfg)
+    return out
+
+
 def small(nx=65, ny=33, kfour=4, kphys=8, msh=3, **kw):
     """A small grid for parity tests (seconds on the CPU oracle)."""
     kw.setdefault("amp3d", 1e-5)

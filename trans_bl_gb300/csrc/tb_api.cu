@@ -140,6 +140,7 @@ int tb_destroy(tb_ctx* c) {
                     c->ry2.w, c->ry2.off, c->ry2.cnt, c->px.lu, c->pfc, c->psc, c->pfct, c->pdef, c->pcarry,
                     c->pstate, c->perr, c->pqdy2, c->pcoef, c->wcoef};
     for (void* p : ptrs) if (p) cudaFree(p);
+    tb_graph_free(c);
     if (c->nl_phys) cudaFree(c->nl_phys);
     for (int q = 0; q < 24; q++) if (c->tmp[q]) cudaFree(c->tmp[q]);
     for (auto& r : c->prof_open) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
@@ -152,6 +153,7 @@ int tb_destroy(tb_ctx* c) {
 int tb_set_coefs(tb_ctx* c, const double* blob) {
     if (!c || !blob) { tb_set_error("null argument"); return TB_ERR_ARG; }
     c->coefs.assign(blob, blob + tb_coef_count(c->g.msh));
+    tb_graph_reset(c);
     int r;
     if ((r = tb_host_build_tables(c))) return r;
     if ((r = tb_poisson_setup(c))) return r;
@@ -165,6 +167,7 @@ int tb_set_baseflow(tb_ctx* c, const double* uxb, const double* uyb, const doubl
     if (!c || !uxb || !uyb || !wzb) { tb_set_error("null argument"); return TB_ERR_ARG; }
     size_t n2 = tb_n2(c);
     c->h_uxb.assign(uxb, uxb + n2); c->h_uyb.assign(uyb, uyb + n2); c->h_wzb.assign(wzb, wzb + n2);
+    tb_graph_reset(c);
     int r = tb_host_upload_baseflow(c);
     if (r) return r;
     c->have_base = true;
@@ -236,7 +239,7 @@ int tb_rk_stage(tb_ctx* c, int stage, int t) {
     if ((r = tb_rk_update(c, stage))) return r;
     if (stage == 1 && (r = tb_ts_pert_k(c, t, 0.5))) return r;
     if (stage == 3 && (r = tb_ts_pert_k(c, t, 1.0))) return r;
-    c->ws_stage = stage; c->ws_t = t;
+    c->ws_stage = stage; c->ws_t = t; c->g_stage = stage;
     if (stage < 4) r = tb_loop_impl(c, c->cfg.tol_stage, false);
     else r = tb_loop_impl(c, c->cfg.tol_final, true);
     c->ws_stage = 0;
@@ -246,6 +249,8 @@ int tb_rk_stage(tb_ctx* c, int stage, int t) {
     return TB_OK;
 }
 int tb_step(tb_ctx* c, int t) {
+    if (!ready(c)) return TB_ERR_STATE;
+    if (tb_graph_usable(c)) return tb_graph_step(c, t);
     for (int s = 1; s <= 4; s++) {
         int r = tb_rk_stage(c, s, t);
         if (r) return r;

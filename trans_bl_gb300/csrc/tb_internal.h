@@ -123,6 +123,19 @@ struct tb_ctx {
     std::vector<cudaEvent_t> prof_pool;
     double prof_ms[16] = {0};
     long long prof_n[16] = {0};
+    // tb_step replayed as a CUDA graph (mixed form): the four stages with each
+    // Poisson solve's correction loop as a conditional WHILE node
+    bool capturing = false;                // launches are being recorded into a graph
+    cudaStream_t body_stream = nullptr;    // records the WHILE bodies
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    double* d_fct = nullptr;               // (2, 4) TS forcing amplitudes of stages 1 and 3
+    int* gsnap = nullptr;                  // (4, 2K) pstate after each stage's solve
+    double* gerr = nullptr;                // (4, K) perr after each stage's solve
+    long long g_outer = 0;                 // kernels of the graph outside the WHILE bodies
+    long long g_body[4] = {0, 0, 0, 0};    // kernels of one body iteration per stage
+    int g_stage = 0;                       // stage being recorded (1..4)
+    long long graph_gen = 0;               // bumped whenever recorded graphs go stale
 };
 
 // Kernel families timed by tb_profile (index into prof_ms / prof_n).
@@ -180,6 +193,19 @@ void tb_chunk_tables(int n, int ny, int S, const double* L1, const double* L2, c
                      const double* ID, double* out);
 inline size_t tb_poi_blk_size(int ny) { return (size_t)9 * ny + 1280; }
 int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro);
+// Step graph support (tb_graph.cu, tb_mixed.cu, tb_spectral.cu)
+int tb_spectral_prepare(tb_ctx* c);               // lazy tables/buffers of the step, made before a capture
+int tb_mixed_graph_pre(tb_ctx* c, int t, cudaStream_t s);   // warm-start continuity before a replay of step t
+void tb_mixed_graph_post(tb_ctx* c, int t);       // after it
+int tb_mixed_absorb_stats(tb_ctx* c, const int* hs, const double* he);   // one solve's pstate/perr into stats
+int tb_ts_pert_fct(tb_ctx* c, int t, double tempt, double* fct);   // forcing amplitudes per forced mode
+int tb_graph_record_step(tb_ctx* c);              // the four stages on c->stream, which is capturing
+int tb_graph_pre(tb_ctx* c, int t, cudaStream_t s);
+int tb_graph_post(tb_ctx* c, const int* hs, const double* he);   // hs (4, 2K), he (4, K) copied from gsnap/gerr
+void tb_graph_reset(tb_ctx* c);                   // drop the recorded graph (tables or buffers changed)
+void tb_graph_free(tb_ctx* c);
+bool tb_graph_usable(const tb_ctx* c);            // tb_step may replay a graph
+int tb_graph_step(tb_ctx* c, int t);
 int tb_mixed_setup(tb_ctx* c);
 void tb_mixed_free(tb_ctx* c);
 void tb_mixed_invalidate(tb_ctx* c);   // forget the warm-start history (new state)

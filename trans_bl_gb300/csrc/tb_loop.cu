@@ -376,14 +376,16 @@ struct PertArgs {
     int nx, ny, i1, i2, nf;
     int mode[4];
     double fct[4];
+    const double* fct_dev;   // when set, the amplitudes are read here (a recorded step graph)
 };
 __global__ void k_ts_pert(PertArgs A) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;  // 0-based
     if (i < A.i1 || i > A.i2 - 2) return;          // 1-based i1+1 .. i2-1
     for (int m = 0; m < A.nf; m++) {
         int k = A.mode[m];
-        A.uy[(size_t)i + (size_t)A.nx * A.ny * k] = make_double2(A.fcx[i] * A.fct[m], 0.0);
-        A.d2uydx2[(size_t)i + (size_t)A.nx * k] = make_double2(A.fcllx[i] * A.fct[m], 0.0);
+        double f = A.fct_dev ? A.fct_dev[m] : A.fct[m];
+        A.uy[(size_t)i + (size_t)A.nx * A.ny * k] = make_double2(A.fcx[i] * f, 0.0);
+        A.d2uydx2[(size_t)i + (size_t)A.nx * k] = make_double2(A.fcllx[i] * f, 0.0);
     }
 }
 
@@ -554,12 +556,11 @@ int tb_wz_wall_k(tb_ctx* c, const cplx* lapv) {
     TB_CHECK_LAUNCH(c);
     return TB_OK;
 }
-int tb_ts_pert_k(tb_ctx* c, int t, double tempt) {
+// Wall-forcing amplitude of each forced mode at step t + tempt, in the order
+// of the forced modes that exist on this grid; returns their number.
+int tb_ts_pert_fct(tb_ctx* c, int t, double tempt, double* out) {
     const tb_config& cf = c->cfg;
-    PertArgs A;
-    std::memset(&A, 0, sizeof A);
-    A.uy = c->uy; A.d2uydx2 = c->d2uydx2; A.fcx = c->fcx; A.fcllx = c->fcllx;
-    A.nx = c->g.nx; A.ny = c->g.ny; A.i1 = cf.i1; A.i2 = cf.i2;
+    int nf = 0;
     for (int m = 0; m < cf.n_forced && m < 4; m++) {
         int k = cf.forced_mode[m];
         if (k < 0 || k >= c->g.K) continue;
@@ -572,8 +573,26 @@ int tb_ts_pert_k(tb_ctx* c, int t, double tempt) {
             double ept = (double)t / (double)cf.stpp;
             fct = fct * ((6.0 * ept - 15.0) * ept + 10.0) * tb_powi(ept, 3);
         }
-        A.mode[A.nf] = k; A.fct[A.nf] = fct; A.nf++;
+        out[nf++] = fct;
     }
+    return nf;
+}
+
+int tb_ts_pert_k(tb_ctx* c, int t, double tempt) {
+    const tb_config& cf = c->cfg;
+    PertArgs A;
+    std::memset(&A, 0, sizeof A);
+    A.uy = c->uy; A.d2uydx2 = c->d2uydx2; A.fcx = c->fcx; A.fcllx = c->fcllx;
+    A.nx = c->g.nx; A.ny = c->g.ny; A.i1 = cf.i1; A.i2 = cf.i2;
+    for (int m = 0; m < cf.n_forced && m < 4; m++) {
+        int k = cf.forced_mode[m];
+        if (k < 0 || k >= c->g.K) continue;
+        A.mode[A.nf++] = k;
+    }
+    tb_ts_pert_fct(c, t, tempt, A.fct);
+    // in a recorded step the amplitudes of stage 1 (tempt 0.5) and stage 3
+    // (tempt 1) are uploaded before each replay
+    if (c->capturing) A.fct_dev = c->d_fct + (tempt < 0.75 ? 0 : 4);
     if (A.nf == 0) return TB_OK;
     k_ts_pert<<<tb_blocks(c->g.nx, 128), 128, 0, c->stream>>>(A);
     TB_CHECK_LAUNCH(c);

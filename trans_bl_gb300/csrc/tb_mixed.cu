@@ -67,9 +67,13 @@ struct Mixed {
     float* qdy2 = nullptr;    // (ny, msh)
     float* ainv = nullptr;    // (K, N, N) inverse of the coarsest operator per mode
     unsigned long long* maxsq = nullptr;   // (K) max |defect|^2 as double bits
-    // warm start: per RK stage the v of the last two steps' solves and their steps
+    // warm start: per RK stage the v of the last two steps' solves (h0 the
+    // newer), how many of them are usable (device, per stage) and the step
+    // of the last solve (host)
     cplx* hist[4][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
-    int hist_t[4][2] = {{-9, -9}, {-9, -9}, {-9, -9}, {-9, -9}};
+    int* hvalid = nullptr;
+    int last_t[4] = {-9, -9, -9, -9};
+    int* iter = nullptr;      // corrections tested so far in a recorded solve loop
     int NL = 0, N = 0;
     int ptsx[MG_MAX], ptsy[MG_MAX], ylvl[MG_MAX], semi[MG_MAX], S[MG_MAX];
     double dx2[MG_MAX];
@@ -427,19 +431,28 @@ __global__ void k_direct(MgDev M) {
     if (lane == 0) M.e[(size_t)k * M.elems + M.off[l] + (size_t)n * (1 + p / m) + 1 + p % m] = f2(ax, ay);
 }
 
-// Warm start: fc = 2 h1 - h2 on the interior of the FP64 fine level (h1, h2:
-// the same stage's v of the two previous steps; the boundary rows and
-// columns keep this stage's Dirichlet data).
-__global__ void k_extrap(cplx* fc, size_t elems64, const cplx* h1, const cplx* h2, int nx, int ny, int K) {
+// Warm start of one stage's solve from its history h0 (previous step), h1
+// (the step before), of which *valid are usable: with both, fc = 2 h0 - h1
+// on the interior of the FP64 fine level (the boundary rows and columns keep
+// this stage's Dirichlet data).  h1 <- h0 then makes room for this solve,
+// which the caller copies into h0.
+__global__ void k_extrap(cplx* fc, size_t elems64, cplx* h0, cplx* h1, const int* valid, int nx, int ny, int K) {
+    const int nv = *valid;
+    if (nv == 0) return;
     size_t per = (size_t)nx * ny;
     size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (q >= per * K) return;
     int k = (int)(q / per);
     int i = (int)((q % per) % nx), j = (int)((q % per) / nx);
-    if (i < 1 || i > nx - 2 || j < 1) return;
-    cplx a = h1[q], b = h2[q];
-    fc[(size_t)k * elems64 + (q % per)] = make_double2(2.0 * a.x - b.x, 2.0 * a.y - b.y);
+    cplx a = h0[q];
+    if (nv >= 2 && i >= 1 && i <= nx - 2 && j >= 1) {
+        cplx b = h1[q];
+        fc[(size_t)k * elems64 + (q % per)] = make_double2(2.0 * a.x - b.x, 2.0 * a.y - b.y);
+    }
+    h1[q] = a;
 }
+
+__global__ void k_hist_count(int* valid) { *valid = min(*valid + 1, 2); }
 
 // u += e on the interior of the FP64 fine level (fc layout: x-contiguous).
 __global__ void k_apply(MgDev M, cplx* fc, size_t elems64, int nx, int ny) {
@@ -469,9 +482,9 @@ __global__ void k_apply(MgDev M, cplx* fc, size_t elems64, int nx, int ny) {
 // into maxsq): converged modes leave the active set with the number of
 // corrections applied; a non-finite defect stops the mode with
 // -1 - corrections.  maxsq is cleared for the next defect.
-__global__ void k_check_sq(unsigned long long* maxsq, int* state, double* err, int K, double tol, int it, int last) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= K || !state[2 * k]) return;
+__device__ __forceinline__ int check_mode(unsigned long long* maxsq, int* state, double* err, int k, double tol, int it,
+                                          int last) {
+    if (!state[2 * k]) return 0;
     double m2 = __longlong_as_double((long long)maxsq[k]);
     maxsq[k] = 0ull;
     double e = sqrt(m2);
@@ -480,6 +493,27 @@ __global__ void k_check_sq(unsigned long long* maxsq, int* state, double* err, i
         err[k] = e;
         if (e < tol) { state[2 * k] = 0; state[2 * k + 1] = it; }
         else if (last) state[2 * k + 1] = it;   // stays active: not converged
+    }
+    return state[2 * k];
+}
+__global__ void k_check_sq(unsigned long long* maxsq, int* state, double* err, int K, double tol, int it, int last) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < K) check_mode(maxsq, state, err, k, tol, it, last);
+}
+// The same test inside a recorded solve (one block): the correction count
+// lives in *iter, and the loop's WHILE condition becomes "some mode is still
+// active and fewer than max_outer corrections were applied".
+constexpr int CHECK_THREADS = 256;
+__global__ void __launch_bounds__(CHECK_THREADS) k_check_loop(unsigned long long* maxsq, int* state, double* err, int K,
+                                                              double tol, int* iter, int first, int max_outer,
+                                                              cudaGraphConditionalHandle h) {
+    const int it = first ? 0 : *iter;
+    int act = 0;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) act |= check_mode(maxsq, state, err, k, tol, it, it == max_outer);
+    act = __syncthreads_or(act);
+    if (threadIdx.x == 0) {
+        *iter = it + 1;
+        cudaGraphSetConditional(h, (act && it < max_outer) ? 1u : 0u);
     }
 }
 
@@ -727,6 +761,13 @@ int tb_mixed_setup(tb_ctx* c) {
     }
     TB_CUDA(cudaMalloc(&m->maxsq, K * sizeof(unsigned long long)));
     TB_CUDA(cudaMemset(m->maxsq, 0, K * sizeof(unsigned long long)));
+    TB_CUDA(cudaMalloc(&m->hvalid, 4 * sizeof(int)));
+    TB_CUDA(cudaMemset(m->hvalid, 0, 4 * sizeof(int)));
+    TB_CUDA(cudaMalloc(&m->iter, sizeof(int)));
+    TB_CUDA(cudaMemset(m->iter, 0, sizeof(int)));
+    if (c->cfg.warm_start)
+        for (auto& h : m->hist)
+            for (cplx*& p : h) TB_CUDA(cudaMalloc(&p, tb_n3(c) * sizeof(cplx)));
     // line-solve tables per (type, level, mode): band5 factors of the level's
     // y-line matrix and chunk tables for this form's rows per lane, in FP32
     const size_t bs = tb_poi_blk_size(ny);
@@ -788,7 +829,21 @@ int tb_mixed_setup(tb_ctx* c) {
 void tb_mixed_invalidate(tb_ctx* c) {
     Mixed* m = get(c);
     if (!m) return;
-    for (auto& h : m->hist_t) { h[0] = -9; h[1] = -9; }
+    for (int& t : m->last_t) t = -9;
+}
+
+int tb_mixed_graph_pre(tb_ctx* c, int t, cudaStream_t s) {
+    Mixed* m = get(c);
+    if (!m) { tb_set_error("mixed form not set up"); return TB_ERR_STATE; }
+    for (int q = 0; q < 4; q++)
+        if (m->last_t[q] != t - 1) TB_CUDA(cudaMemsetAsync(m->hvalid + q, 0, sizeof(int), s));
+    return TB_OK;
+}
+
+void tb_mixed_graph_post(tb_ctx* c, int t) {
+    Mixed* m = get(c);
+    if (m && c->cfg.warm_start)
+        for (int& q : m->last_t) q = t;
 }
 
 void tb_mixed_free(tb_ctx* c) {
@@ -798,64 +853,82 @@ void tb_mixed_free(tb_ctx* c) {
         for (cplx* p : h)
             if (p) cudaFree(p);
     for (void* p : {(void*)m->e, (void*)m->r, (void*)m->rr, (void*)m->tab, (void*)m->coef, (void*)m->qdy2, (void*)m->ainv,
-                    (void*)m->maxsq})
+                    (void*)m->maxsq, (void*)m->hvalid, (void*)m->iter})
         if (p) cudaFree(p);
     delete m;
     c->mixed = nullptr;
 }
 
-// poi_uy (poisson_par.f:6-64), mixed form: at most max_vcycles FP64
-// corrections per solve; stats.vcycles[k] counts the corrections applied to
-// mode k.
-int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
-    if (!c->mixed) { tb_set_error("mixed form not set up"); return TB_ERR_STATE; }
-    const int K = c->g.K, nx = c->g.nx, ny = c->g.ny, max_outer = c->cfg.max_vcycles;
-    MgDev M = make(c);
+// One FP64 correction recorded as the body of the solve's WHILE node:
+// INNER_VCYCLES V-cycles of the FP32 hierarchy, u += e, the new defect and
+// its test (which sets the loop condition).
+static int record_body(tb_ctx* c, const MgDev& M, double erro, cudaGraphConditionalHandle h) {
+    Mixed* m = get(c);
     int r;
-    cudaEvent_t pall = nullptr;
-    if ((r = tb_prof_begin(c, PROF_POISSON, &pall))) return r;
-    if ((r = tb_poisson_begin(c, dwzdx))) return r;
-    Mixed* mx = get(c);
-    const int ws = (c->cfg.warm_start && c->ws_stage >= 1 && c->ws_stage <= 4) ? c->ws_stage - 1 : -1;
-    if (ws >= 0) {
-        for (cplx*& h : mx->hist[ws])
-            if (!h) TB_CUDA(cudaMalloc(&h, tb_n3(c) * sizeof(cplx)));
-        if (mx->hist_t[ws][0] == c->ws_t - 1 && mx->hist_t[ws][1] == c->ws_t - 2) {
-            k_extrap<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(c->pfc, c->g.lvl_elems, mx->hist[ws][0],
-                                                                      mx->hist[ws][1], nx, ny, K);
-            TB_CHECK_LAUNCH(c);
-        }
+    for (int v = 0; v < INNER_VCYCLES; v++)
+        if ((r = vcycle(c, M))) return r;
+    dim3 tgrid(tb_blocks(c->g.nx, 32), tb_blocks(c->g.ny, 32), c->g.K), tblk(32, 8);
+    k_apply<<<tgrid, tblk, 0, c->stream>>>(M, c->pfc, c->g.lvl_elems, c->g.nx, c->g.ny);
+    TB_CHECK_LAUNCH(c);
+    if ((r = tb_poisson_defect_f32(c, m->r, m->e, m->elems, m->maxsq))) return r;
+    k_check_loop<<<1, CHECK_THREADS, 0, c->stream>>>(m->maxsq, c->pstate, c->perr, c->g.K, erro, m->iter, 0,
+                                                     c->cfg.max_vcycles, h);
+    TB_CHECK_LAUNCH(c);
+    return TB_OK;
+}
+
+// The correction loop of a solve being recorded into a step graph: first
+// defect and test, then a conditional WHILE node that repeats the body
+// above until every mode has converged or max_vcycles corrections ran.
+static int record_loop(tb_ctx* c, const MgDev& M, double erro) {
+    Mixed* m = get(c);
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    TB_CUDA(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, nullptr, nullptr, nullptr));
+    if (st != cudaStreamCaptureStatusActive || !g) { tb_set_error("step graph: stream is not recording"); return TB_ERR_STATE; }
+    cudaGraphConditionalHandle h;
+    TB_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+    int r;
+    if ((r = tb_poisson_defect_f32(c, m->r, m->e, m->elems, m->maxsq))) return r;
+    k_check_loop<<<1, CHECK_THREADS, 0, c->stream>>>(m->maxsq, c->pstate, c->perr, c->g.K, erro, m->iter, 1,
+                                                     c->cfg.max_vcycles, h);
+    TB_CHECK_LAUNCH(c);
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    TB_CUDA(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphNodeParams p = {};
+    std::memset(&p, 0, sizeof p);
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    TB_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+    TB_CUDA(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    cudaStream_t outer = c->stream;
+    c->stream = c->body_stream;
+    const long long l0 = c->launches;
+    cudaError_t e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) {
+        c->stream = outer;
+        tb_set_error("step graph: recording the solve loop: %s", cudaGetErrorString(e));
+        return TB_ERR_CUDA;
     }
-    std::vector<int> hs(2 * K);
-    dim3 tgrid(tb_blocks(nx, 32), tb_blocks(ny, 32), K), tblk(32, 8);
-    for (int it = 0; it <= max_outer; it++) {
-        Mixed* m = get(c);
-        if ((r = tb_poisson_defect_f32(c, m->r, m->e, m->elems, m->maxsq))) return r;
-        k_check_sq<<<tb_blocks(K, 64), 64, 0, c->stream>>>(m->maxsq, c->pstate, c->perr, K, erro, it, it == max_outer);
-        TB_CHECK_LAUNCH(c);
-        if (it == max_outer) break;
-        TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-        TB_CUDA(cudaStreamSynchronize(c->stream));
-        bool any = false;
-        for (int k = 0; k < K; k++) any = any || hs[2 * k];
-        if (!any) break;
-        for (int v = 0; v < INNER_VCYCLES; v++)
-            if ((r = vcycle(c, M))) return r;
-        k_apply<<<tgrid, tblk, 0, c->stream>>>(M, c->pfc, c->g.lvl_elems, nx, ny);
-        TB_CHECK_LAUNCH(c);
-    }
-    if ((r = tb_poisson_end(c))) return r;
-    if (ws >= 0) {   // keep this solve for the next steps' guesses
-        std::swap(mx->hist[ws][0], mx->hist[ws][1]);
-        TB_CUDA(cudaMemcpyAsync(mx->hist[ws][0], c->uy, tb_n3(c) * sizeof(cplx), cudaMemcpyDeviceToDevice, c->stream));
-        mx->hist_t[ws][1] = mx->hist_t[ws][0];
-        mx->hist_t[ws][0] = c->ws_t;
-    }
-    if ((r = tb_prof_end(c, PROF_POISSON, pall))) return r;
-    std::vector<double> he(K);
-    TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    TB_CUDA(cudaMemcpyAsync(he.data(), c->perr, K * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    TB_CUDA(cudaStreamSynchronize(c->stream));
+    r = record_body(c, M, erro, h);
+    cudaGraph_t got = nullptr;
+    e = cudaStreamEndCapture(c->stream, &got);
+    c->stream = outer;
+    if (r) return r;
+    if (e != cudaSuccess) { tb_set_error("step graph: recording the solve loop: %s", cudaGetErrorString(e)); return TB_ERR_CUDA; }
+    if (c->g_stage >= 1 && c->g_stage <= 4) c->g_body[c->g_stage - 1] = c->launches - l0;
+    return TB_OK;
+}
+
+// One solve's per-mode state (hs: active flag and corrections, per mode)
+// and final defect (he) into the statistics.
+int tb_mixed_absorb_stats(tb_ctx* c, const int* hs, const double* he) {
+    const int K = c->g.K;
     c->stats.noconv = 0;
     int nonfinite = 0;
     for (int k = 0; k < K && k < 256; k++) {
@@ -869,4 +942,71 @@ int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
     c->stats.solves++;
     if (nonfinite) { tb_set_error("poi_uy (mixed form): non-finite defect"); return TB_ERR_NONFINITE; }
     return TB_OK;
+}
+
+// poi_uy (poisson_par.f:6-64), mixed form: at most max_vcycles FP64
+// corrections per solve; stats.vcycles[k] counts the corrections applied to
+// mode k.
+int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
+    if (!c->mixed) { tb_set_error("mixed form not set up"); return TB_ERR_STATE; }
+    const int K = c->g.K, nx = c->g.nx, ny = c->g.ny, max_outer = c->cfg.max_vcycles;
+    MgDev M = make(c);
+    Mixed* mx = get(c);
+    int r;
+    cudaEvent_t pall = nullptr;
+    if ((r = tb_prof_begin(c, PROF_POISSON, &pall))) return r;
+    if ((r = tb_poisson_begin(c, dwzdx))) return r;
+    const int ws = (c->cfg.warm_start && c->ws_stage >= 1 && c->ws_stage <= 4) ? c->ws_stage - 1 : -1;
+    if (ws >= 0) {
+        // a recorded step checks the continuity of its steps before each replay
+        if (!c->capturing && mx->last_t[ws] != c->ws_t - 1)
+            TB_CUDA(cudaMemsetAsync(mx->hvalid + ws, 0, sizeof(int), c->stream));
+        k_extrap<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(c->pfc, c->g.lvl_elems, mx->hist[ws][0],
+                                                                  mx->hist[ws][1], mx->hvalid + ws, nx, ny, K);
+        TB_CHECK_LAUNCH(c);
+    }
+    if (c->capturing) {
+        if ((r = record_loop(c, M, erro))) return r;
+    } else {
+        std::vector<int> hs(2 * K);
+        dim3 tgrid(tb_blocks(nx, 32), tb_blocks(ny, 32), K), tblk(32, 8);
+        for (int it = 0; it <= max_outer; it++) {
+            Mixed* m = get(c);
+            if ((r = tb_poisson_defect_f32(c, m->r, m->e, m->elems, m->maxsq))) return r;
+            k_check_sq<<<tb_blocks(K, 64), 64, 0, c->stream>>>(m->maxsq, c->pstate, c->perr, K, erro, it, it == max_outer);
+            TB_CHECK_LAUNCH(c);
+            if (it == max_outer) break;
+            TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+            TB_CUDA(cudaStreamSynchronize(c->stream));
+            bool any = false;
+            for (int k = 0; k < K; k++) any = any || hs[2 * k];
+            if (!any) break;
+            for (int v = 0; v < INNER_VCYCLES; v++)
+                if ((r = vcycle(c, M))) return r;
+            k_apply<<<tgrid, tblk, 0, c->stream>>>(M, c->pfc, c->g.lvl_elems, nx, ny);
+            TB_CHECK_LAUNCH(c);
+        }
+    }
+    if ((r = tb_poisson_end(c))) return r;
+    if (ws >= 0) {   // this solve becomes the newest entry of the stage's history
+        TB_CUDA(cudaMemcpyAsync(mx->hist[ws][0], c->uy, tb_n3(c) * sizeof(cplx), cudaMemcpyDeviceToDevice, c->stream));
+        k_hist_count<<<1, 1, 0, c->stream>>>(mx->hvalid + ws);
+        TB_CHECK_LAUNCH(c);
+        if (!c->capturing) mx->last_t[ws] = c->ws_t;
+    }
+    if ((r = tb_prof_end(c, PROF_POISSON, pall))) return r;
+    if (c->capturing) {   // the step's statistics are read after each replay
+        const int s = c->g_stage - 1;
+        if (s < 0 || s > 3) { tb_set_error("step graph: solve outside a stage"); return TB_ERR_STATE; }
+        TB_CUDA(cudaMemcpyAsync(c->gsnap + (size_t)2 * K * s, c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToDevice,
+                                c->stream));
+        TB_CUDA(cudaMemcpyAsync(c->gerr + (size_t)K * s, c->perr, K * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        return TB_OK;
+    }
+    std::vector<int> hs(2 * K);
+    std::vector<double> he(K);
+    TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TB_CUDA(cudaMemcpyAsync(he.data(), c->perr, K * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    TB_CUDA(cudaStreamSynchronize(c->stream));
+    return tb_mixed_absorb_stats(c, hs.data(), he.data());
 }

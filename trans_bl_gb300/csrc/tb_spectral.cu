@@ -492,6 +492,14 @@ int tb_launch_p_to_f(tb_ctx* c, cplx* four, const double* phys) {
     TB_CHECK_LAUNCH(c);
     return TB_OK;
 }
+int tb_spectral_prepare(tb_ctx* c) {
+    int r = ensure_twiddles(c);
+    if (r) return r;
+    if (c->cfg.precision == TB_FORM_MIXED && c->g.P >= 4 && !c->nl_phys)
+        TB_CUDA(cudaMalloc(&c->nl_phys, (size_t)6 * c->g.P * tb_n2(c) * sizeof(float)));
+    return TB_OK;
+}
+
 int tb_launch_nlterms(tb_ctx* c, cplx* a, cplx* b, cplx* cc) {
     int r = ensure_twiddles(c);
     if (r) return r;
