@@ -50,6 +50,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
+    p.add_argument("--no-ensemble", action="store_true", help="skip the 12-run ensemble measurement")
     return p.parse_args()
 
 
@@ -353,6 +354,8 @@ def main():
     if rank == 0 and world == 1 and form == "mixed" and not args.no_plain and state2 is not None:
         line["plain_fp64"] = plain_comparison(coefs, base, state2, t0, hbm_peak)
         line["speedup_vs_plain"] = value / line["plain_fp64"]["value"]
+    if rank == 0 and world == 1 and form == "mixed" and not args.no_ensemble:
+        line["ensemble"] = ensemble_measure(max(1, min(args.steps, 5)), 3)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         pcfg = workload("plain")
         threads = os.cpu_count() or 1
@@ -363,6 +366,60 @@ def main():
                                           "(%.2f s); per-step rate = stage rate / 4" % (used, cpu_s)}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def ensemble_measure(steps, warmup):
+    """The 12 uneven runs of the ensemble workload from disturbed states past
+    their forcing ramps: advanced together (one graph launch per step for all
+    members) and, from the same states, one member after another (each its
+    own step graph).  Host wall time over `steps` steps; both end every step
+    with a host wait, as the API does."""
+    from trans_bl_gb300 import api, configs
+    cfgs = configs.config3(precision=api.FORM_MIXED)
+    ctxs, starts = [], []
+    for cfg in cfgs:
+        coefs, base = configs.setup_inputs(cfg)
+        g = api.Context(cfg, coefs, base)
+        st = start_state(cfg, base)
+        g.put_state(st)
+        ctxs.append(g)
+        starts.append(st)
+    pts = sum(c.nx * c.ny * c.kfour for c in cfgs)
+    t = [c.stpp + 1 for c in cfgs]
+    ens = api.Ensemble(ctxs)
+    for _ in range(warmup):
+        ens.step(t)
+        t = [v + 1 for v in t]
+    vc0 = sum(g.poisson_stats()["total_vcycles"] for g in ctxs)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ens.step(t)
+        t = [v + 1 for v in t]
+    el_b = time.perf_counter() - t0
+    vc = sum(g.poisson_stats()["total_vcycles"] for g in ctxs) - vc0
+    ens.close()
+    t = [c.stpp + 1 for c in cfgs]
+    for g, st in zip(ctxs, starts):
+        g.put_state(st)
+    for _ in range(warmup):
+        for q, g in enumerate(ctxs):
+            g.step(t[q])
+        t = [v + 1 for v in t]
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for q, g in enumerate(ctxs):
+            g.step(t[q])
+        t = [v + 1 for v in t]
+    el_s = time.perf_counter() - t0
+    for g in ctxs:
+        g.close()
+    members = ["%dx%dx%d F=%.3g stpp=%d" % (c.nx, c.ny, c.kfour, c.omega / c.Re, c.stpp) for c in cfgs]
+    return {"workload": "ensemble of 12 uneven runs (nx 257-1025, ny 97-193, kfour 8-32, F 0.6-1.4e-4)",
+            "members": members, "points": pts, "steps": steps, "warmup": warmup,
+            "value": pts * steps / el_b / 1e6, "unit": "Mpt-steps/s", "ms_per_step": 1e3 * el_b / steps,
+            "one_after_another": {"value": pts * steps / el_s / 1e6, "ms_per_step": 1e3 * el_s / steps},
+            "speedup_vs_one_after_another": el_s / el_b, "timing": "host wall clock per ensemble step",
+            "corrections_per_step": vc / steps}
 
 
 def sor_points_per_launch(cfg):
