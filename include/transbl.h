@@ -173,6 +173,40 @@ int tb_step(tb_ctx* ctx, int t);                  /* four stages                
 int tb_steps(tb_ctx* ctx, int t0, int nsteps);    /* t0 .. t0+nsteps-1           */
 int tb_get_poisson_stats(tb_ctx* ctx, tb_poisson_stats* st);
 
+/* ---- learned first correction of the mixed v-Poisson solve ------------
+   A convolutional network (four 3x3 layers, 4 -> 32 -> 32 -> 32 -> 1
+   channels, GELU) estimates, per mode, the error of the extrapolated guess
+   from v(t-1), v(t-1) - v(t-2) and the FP64 defect of the guess.  Its
+   correction is kept per mode only where it lowers the max defect; the
+   multigrid then iterates to the same tolerance.  The solver generates the
+   training crops itself, and the network is trained on the GPU by the
+   library's own forward and backward kernels (Adam).  Needs the mixed form
+   with warm_start = 1.  Crops are collected only from host-launched steps:
+   while collecting, tb_step does not replay a graph.                      */
+typedef struct tb_learn_stats {
+    long long samples;     /* training crops collected                          */
+    long long capacity;    /* crops the sample buffer holds                     */
+    long long tried;       /* mode-solves that evaluated the network            */
+    long long kept;        /* of those, corrections kept (the rest fell back)   */
+    double    loss;        /* mean training loss over the last tenth of training */
+} tb_learn_stats;
+int tb_learn_param_count(void);                 /* floats in a weight vector        */
+int tb_learn_crop_size(void);                   /* edge of a training crop (72)     */
+int tb_learn_init(tb_ctx* ctx, unsigned long long seed);   /* He-normal, last layer 0 */
+int tb_learn_set_weights(tb_ctx* ctx, const float* w);
+int tb_learn_get_weights(tb_ctx* ctx, float* w);
+int tb_learn_enable(tb_ctx* ctx, int on);       /* apply the network in every solve */
+/* Collect crops_per_solve crops from every solve into a buffer of `capacity`
+   crops; capacity 0 stops collecting and keeps the crops for training.     */
+int tb_learn_sample(tb_ctx* ctx, long long capacity, int crops_per_solve, unsigned long long seed);
+int tb_learn_train(tb_ctx* ctx, int iters, int batch, float lr, unsigned long long seed, double* loss);
+int tb_learn_get_stats(tb_ctx* ctx, tb_learn_stats* st);
+/* The training kernels on caller data (host memory, current device):
+   loss and gradient over n crops (n, 5, 72, 72), planes 0-3 the inputs and
+   plane 4 the target; and the network's output on n images (n, 4, H, W).  */
+int tb_learn_grad(const float* w, const float* crops, int n, double* loss, float* grad);
+int tb_learn_forward(const float* w, const float* x, int n, int H, int W, float* out);
+
 /* ---- ensembles: independent runs advanced together --------------------
    One recorded CUDA graph advances every member by one step: the members'
    stages run concurrently on the device and the host waits once per step.

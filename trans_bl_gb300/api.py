@@ -51,6 +51,11 @@ class LstConfig(C.Structure):
         [("imax", C.c_int), ("dx", C.c_double), ("steps", C.c_int)]
 
 
+class LearnStats(C.Structure):
+    _fields_ = [("samples", C.c_longlong), ("capacity", C.c_longlong), ("tried", C.c_longlong),
+                ("kept", C.c_longlong), ("loss", C.c_double)]
+
+
 class TbError(RuntimeError):
     pass
 
@@ -113,6 +118,16 @@ def load():
     lib.tb_read_checkpoint.argtypes = [P, C.c_char_p, C.POINTER(C.c_int)]
     lib.tb_write_pert.argtypes = [P, C.c_char_p]
     lib.tb_io_set_subrecord_limit.argtypes = [C.c_longlong]
+    F = C.POINTER(C.c_float)
+    lib.tb_learn_init.argtypes = [P, C.c_ulonglong]
+    lib.tb_learn_set_weights.argtypes = [P, F]
+    lib.tb_learn_get_weights.argtypes = [P, F]
+    lib.tb_learn_enable.argtypes = [P, C.c_int]
+    lib.tb_learn_sample.argtypes = [P, C.c_longlong, C.c_int, C.c_ulonglong]
+    lib.tb_learn_train.argtypes = [P, C.c_int, C.c_int, C.c_float, C.c_ulonglong, D]
+    lib.tb_learn_get_stats.argtypes = [P, C.POINTER(LearnStats)]
+    lib.tb_learn_grad.argtypes = [F, F, C.c_int, D, F]
+    lib.tb_learn_forward.argtypes = [F, F, C.c_int, C.c_int, C.c_int, F]
     lib.tb_ensemble_create.argtypes = [C.POINTER(P), C.c_int, C.POINTER(P)]
     lib.tb_ensemble_step.argtypes = [P, C.POINTER(C.c_int)]
     lib.tb_ensemble_destroy.argtypes = [P]
@@ -142,6 +157,39 @@ def default_config(**kw):
         else:
             setattr(cfg, k, v)
     return cfg
+
+
+def fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def learn_param_count():
+    return int(load().tb_learn_param_count())
+
+
+def learn_crop_size():
+    return int(load().tb_learn_crop_size())
+
+
+def learn_grad(w, crops):
+    """Loss and gradient of the learned-correction network on crops
+    (n, 5, 72, 72) float32, computed by the library's training kernels."""
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    crops = np.ascontiguousarray(crops, dtype=np.float32)
+    g = np.zeros(learn_param_count(), dtype=np.float32)
+    loss = np.zeros(1)
+    check(load().tb_learn_grad(fptr(w), fptr(crops), crops.shape[0], dptr(loss), fptr(g)), "tb_learn_grad")
+    return float(loss[0]), g
+
+
+def learn_forward(w, x):
+    """The network's output (n, H, W) on inputs x (n, 4, H, W) float32."""
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    n, _, H, W = x.shape
+    out = np.zeros((n, H, W), dtype=np.float32)
+    check(load().tb_learn_forward(fptr(w), fptr(x), n, H, W, fptr(out)), "tb_learn_forward")
+    return out
 
 
 def coef_count(msh):
@@ -283,6 +331,37 @@ class Context:
 
     def write_pert(self, path):
         self._c(self.lib.tb_write_pert(self.h, os.fsencode(path)), "tb_write_pert")
+
+    # learned first correction ----------------------------------------------
+    def learn_init(self, seed=1):
+        self._c(self.lib.tb_learn_init(self.h, seed), "tb_learn_init")
+
+    def learn_weights(self):
+        w = np.zeros(learn_param_count(), dtype=np.float32)
+        self._c(self.lib.tb_learn_get_weights(self.h, fptr(w)), "tb_learn_get_weights")
+        return w
+
+    def learn_set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        if w.size != learn_param_count():
+            raise ValueError("expected %d weights" % learn_param_count())
+        self._c(self.lib.tb_learn_set_weights(self.h, fptr(w)), "tb_learn_set_weights")
+
+    def learn_enable(self, on=True):
+        self._c(self.lib.tb_learn_enable(self.h, 1 if on else 0), "tb_learn_enable")
+
+    def learn_sample(self, capacity, crops_per_solve=16, seed=1):
+        self._c(self.lib.tb_learn_sample(self.h, int(capacity), int(crops_per_solve), seed), "tb_learn_sample")
+
+    def learn_train(self, iters, batch=32, lr=1e-3, seed=1):
+        loss = np.zeros(1)
+        self._c(self.lib.tb_learn_train(self.h, int(iters), int(batch), float(lr), seed, dptr(loss)), "tb_learn_train")
+        return float(loss[0])
+
+    def learn_stats(self):
+        st = LearnStats()
+        self._c(self.lib.tb_learn_get_stats(self.h, C.byref(st)), "tb_learn_get_stats")
+        return {n: getattr(st, n) for n, _ in LearnStats._fields_}
 
     def profile(self, enable):
         self._c(self.lib.tb_profile(self.h, 1 if enable else 0), "tb_profile")

@@ -141,6 +141,7 @@ int tb_destroy(tb_ctx* c) {
                     c->pstate, c->perr, c->pqdy2, c->pcoef, c->wcoef};
     for (void* p : ptrs) if (p) cudaFree(p);
     tb_graph_free(c);
+    tb_learn_free(c);
     if (c->nl_phys) cudaFree(c->nl_phys);
     for (int q = 0; q < 24; q++) if (c->tmp[q]) cudaFree(c->tmp[q]);
     for (auto& r : c->prof_open) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
@@ -154,6 +155,7 @@ int tb_set_coefs(tb_ctx* c, const double* blob) {
     if (!c || !blob) { tb_set_error("null argument"); return TB_ERR_ARG; }
     c->coefs.assign(blob, blob + tb_coef_count(c->g.msh));
     tb_graph_reset(c);
+    tb_learn_free(c);   // its operator tables follow the coefficients
     int r;
     if ((r = tb_host_build_tables(c))) return r;
     if ((r = tb_poisson_setup(c))) return r;

@@ -150,7 +150,11 @@ void tb_graph_free(tb_ctx* c) {
     c->d_fct = nullptr; c->gsnap = nullptr; c->gerr = nullptr; c->body_stream = nullptr;
 }
 
-bool tb_graph_usable(const tb_ctx* c) { return c->cfg.step_graph && graph_form(c) && !c->prof; }
+bool tb_graph_usable(const tb_ctx* c) {
+    // collecting training crops draws crop positions on the host per solve
+    LearnSolve* L = tb_learn_solve(const_cast<tb_ctx*>(c));
+    return c->cfg.step_graph && graph_form(c) && !c->prof && !(L && L->sample);
+}
 
 int tb_graph_step(tb_ctx* c, int t) {
     int r;
@@ -271,6 +275,8 @@ int tb_ensemble_step(tb_ensemble* e, const int* t) {
     bool stale = !e->x;
     for (size_t i = 0; i < e->m.size(); i++) {
         if (e->m[i]->prof) { tb_set_error("ensemble member %zu is profiling", i); return TB_ERR_STATE; }
+        LearnSolve* L = tb_learn_solve(e->m[i]);
+        if (L && L->sample) { tb_set_error("ensemble member %zu is collecting training crops", i); return TB_ERR_STATE; }
         stale = stale || e->gen[i] != e->m[i]->graph_gen;
     }
     if (stale) {

@@ -136,6 +136,7 @@ struct tb_ctx {
     long long g_body[4] = {0, 0, 0, 0};    // kernels of one body iteration per stage
     int g_stage = 0;                       // stage being recorded (1..4)
     long long graph_gen = 0;               // bumped whenever recorded graphs go stale
+    void* learn = nullptr;                 // learned first correction (tb_learn.cu)
 };
 
 // Kernel families timed by tb_profile (index into prof_ms / prof_n).
@@ -193,6 +194,26 @@ void tb_chunk_tables(int n, int ny, int S, const double* L1, const double* L2, c
                      const double* ID, double* out);
 inline size_t tb_poi_blk_size(int ny) { return (size_t)9 * ny + 1280; }
 int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro);
+// Learned first correction of the mixed solve (tb_learn.cu owns the network
+// and buffers, tb_mixed.cu the solver-side kernels).
+struct LearnSolve {
+    bool infer = false;          // apply the network's correction in every solve
+    bool sample = false;         // collect training crops from every solve
+    float* X = nullptr;          // (2K, 4, nx, ny) network input planes per mode and part
+    float* out = nullptr;        // (2K, nx, ny) network output
+    float* scl = nullptr;        // (K, 3) input scales: max|v1|, max|v1 - v2|, max|D^-1 d0|
+    unsigned* jmax = nullptr;    // (K) max |r - L e|^2 of the candidate correction, float bits
+    float* invD = nullptr;       // (K, ny) 1 / |diagonal| of the fine line operator
+    float* mfeat = nullptr;      // (K, ny) share of k^2 beta^2 in the diagonal
+    cplx* g0 = nullptr;          // guess before any correction (while sampling)
+    long long* tally = nullptr;  // (K, 2) solves tried / corrections kept per mode
+};
+LearnSolve* tb_learn_solve(tb_ctx* c);     // null unless the learned form is on
+int tb_learn_run_net(tb_ctx* c);           // X -> out on c->stream
+int tb_learn_collect(tb_ctx* c);           // this solve's crops into the sample buffer
+void tb_learn_free(tb_ctx* c);
+int tb_mixed_line_diag(tb_ctx* c, std::vector<float>& invD, std::vector<float>& mfeat);
+
 // Step graph support (tb_graph.cu, tb_mixed.cu, tb_spectral.cu)
 int tb_spectral_prepare(tb_ctx* c);               // lazy tables/buffers of the step, made before a capture
 int tb_mixed_graph_pre(tb_ctx* c, int t, cudaStream_t s);   // warm-start continuity before a replay of step t

@@ -73,6 +73,8 @@ struct Mixed {
     cplx* hist[4][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
     int* hvalid = nullptr;
     int last_t[4] = {-9, -9, -9, -9};
+    int hv_host[4] = {0, 0, 0, 0};   // host copy of hvalid for host-launched solves
+    int* lkeep = nullptr;            // (K, 2) learned correction kept per mode, in the layout of pstate
     int* iter = nullptr;      // corrections tested so far in a recorded solve loop
     int NL = 0, N = 0;
     int ptsx[MG_MAX], ptsy[MG_MAX], ylvl[MG_MAX], semi[MG_MAX], S[MG_MAX];
@@ -436,7 +438,8 @@ __global__ void k_direct(MgDev M) {
 // on the interior of the FP64 fine level (the boundary rows and columns keep
 // this stage's Dirichlet data).  h1 <- h0 then makes room for this solve,
 // which the caller copies into h0.
-__global__ void k_extrap(cplx* fc, size_t elems64, cplx* h0, cplx* h1, const int* valid, int nx, int ny, int K) {
+__global__ void k_extrap(cplx* fc, size_t elems64, cplx* h0, cplx* h1, const int* valid, int nx, int ny, int K,
+                         int shift) {
     const int nv = *valid;
     if (nv == 0) return;
     size_t per = (size_t)nx * ny;
@@ -449,7 +452,126 @@ __global__ void k_extrap(cplx* fc, size_t elems64, cplx* h0, cplx* h1, const int
         cplx b = h1[q];
         fc[(size_t)k * elems64 + (q % per)] = make_double2(2.0 * a.x - b.x, 2.0 * a.y - b.y);
     }
-    h1[q] = a;
+    if (shift) h1[q] = a;
+}
+
+// ---- learned first correction (network and training in tb_learn.cu) -------
+// Per mode maxima over both parts of |v1| and |v1 - v2| (history,
+// x-contiguous) and of |D^-1 d0| (d0: the FP32 copy r of the FP64 defect of
+// the guess, line-contiguous), as float bits in scl (K, 3).
+__global__ void k_learn_scale(MgDev M, const cplx* h0, const cplx* h1, const int* valid, unsigned* scl, const float* invD,
+                              int nx) {
+    if (*valid < 2) return;
+    const int k = blockIdx.y, ny = M.ny;
+    const size_t per = (size_t)nx * ny;
+    float a = 0.f, b = 0.f, d = 0.f;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < per; q += (size_t)gridDim.x * blockDim.x) {
+        const cplx u = h0[(size_t)k * per + q], w = h1[(size_t)k * per + q];
+        a = fmaxf(a, fmaxf(fabsf((float)u.x), fabsf((float)u.y)));
+        b = fmaxf(b, fmaxf(fabsf((float)(u.x - w.x)), fabsf((float)(u.y - w.y))));
+        const float2 r = M.r[(size_t)k * M.elems + M.off[0] + q];   // point (q / ny, q % ny)
+        d = fmaxf(d, invD[(size_t)k * ny + q % ny] * fmaxf(fabsf(r.x), fabsf(r.y)));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+        b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+        d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&scl[3 * k], __float_as_uint(a));
+        atomicMax(&scl[3 * k + 1], __float_as_uint(b));
+        atomicMax(&scl[3 * k + 2], __float_as_uint(d));
+    }
+}
+
+// The network's input planes X (2K, 4, nx, ny) and the history shift
+// h1 <- h0 that k_extrap leaves to this kernel when the network runs.
+__global__ void k_learn_prep(MgDev M, const cplx* h0, cplx* h1, const int* valid, const float* scl, const float* invD,
+                             const float* mfeat, float* X, int nx) {
+    const int nv = *valid;
+    if (nv == 0) return;
+    __shared__ float2 t0[32][33], t1[32][33];   // [j][i]: v1, v1 - v2
+    const int k = blockIdx.z, ny = M.ny, i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+    const size_t per = (size_t)nx * ny;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int i = i0 + threadIdx.x, j = j0 + r;
+        float2 a = f2(0.f, 0.f), b = f2(0.f, 0.f);
+        if (i < nx && j < ny) {
+            const size_t o = (size_t)k * per + (size_t)j * nx + i;
+            const cplx u = h0[o], w = h1[o];
+            a = f2((float)u.x, (float)u.y);
+            b = f2((float)(u.x - w.x), (float)(u.y - w.y));
+            h1[o] = u;
+        }
+        t0[r][threadIdx.x] = a;
+        t1[r][threadIdx.x] = b;
+    }
+    if (nv < 2) return;   // uniform over the block
+    __syncthreads();
+    const float sv = scl[3 * k], si = scl[3 * k + 1], sd = scl[3 * k + 2];
+    const float iv = sv > 0.f ? 1.f / sv : 0.f, ii = si > 0.f ? 1.f / si : 0.f, id = sd > 0.f ? 1.f / sd : 0.f;
+    float* Xr = X + (size_t)(2 * k) * 4 * per;   // planes of the real part, then of the imaginary part
+    float* Xi = Xr + 4 * per;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int i = i0 + r, j = j0 + threadIdx.x;
+        if (i >= nx || j >= ny) continue;
+        const float2 a = t0[threadIdx.x][r], b = t1[threadIdx.x][r];
+        const float2 d = M.r[(size_t)k * M.elems + M.off[0] + (size_t)ny * i + j];
+        const float sj = invD[(size_t)k * ny + j] * id, mf = mfeat[(size_t)k * ny + j];
+        const size_t o = (size_t)ny * i + j;
+        Xr[o] = a.x * iv; Xr[per + o] = b.x * ii; Xr[2 * per + o] = d.x * sj; Xr[3 * per + o] = mf;
+        Xi[o] = a.y * iv; Xi[per + o] = b.y * ii; Xi[2 * per + o] = d.y * sj; Xi[3 * per + o] = mf;
+    }
+}
+
+// Candidate correction e = max|v1 - v2| * network output on the fine interior.
+__global__ void k_learn_emit(MgDev M, const float* out, const float* scl, const int* valid, int nx) {
+    if (*valid < 2) return;
+    const int ny = M.ny;
+    const size_t per = (size_t)(nx - 2) * (ny - 1), img = (size_t)nx * ny;
+    const size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * M.K) return;
+    const int k = (int)(q / per);
+    const size_t rq = q % per;
+    const int j = 1 + (int)(rq % (ny - 1)), i = 1 + (int)(rq / (ny - 1));
+    const float s = scl[3 * k + 1];
+    const size_t o = (size_t)ny * i + j;
+    M.e[(size_t)k * M.elems + M.off[0] + o] = f2(s * out[(size_t)(2 * k) * img + o], s * out[(size_t)(2 * k + 1) * img + o]);
+}
+
+// max |r - L e|^2 per mode (blockIdx.y) over the fine interior, float bits.
+__global__ void k_learn_judge(MgDev M, unsigned* jmax, const int* valid, int nx) {
+    if (*valid < 2) return;
+    const int k = blockIdx.y, ny = M.ny;
+    const size_t per = (size_t)(nx - 2) * (ny - 1);
+    float m = 0.f;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < per; q += (size_t)gridDim.x * blockDim.x) {
+        const int j = 1 + (int)(q % (ny - 1)), i = 1 + (int)(q / (ny - 1));
+        const float2 v = M.rr[(size_t)k * M.elems + M.off[0] + (size_t)ny * i + j];
+        m = fmaxf(m, v.x * v.x + v.y * v.y);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&jmax[k], __float_as_uint(m));
+}
+
+// Keep the candidate for a mode when it lowers the max defect; count the
+// solves tried and the corrections kept; clear the maxima for the loop.
+__global__ void k_learn_keep(unsigned long long* maxsq, unsigned* jmax, int* keep, long long* tally, const int* valid,
+                             int K) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    int ok = 0;
+    if (*valid >= 2) {
+        const double d0 = __longlong_as_double((long long)maxsq[k]);
+        const double d1 = (double)__uint_as_float(jmax[k]);
+        ok = d1 < d0;
+        tally[2 * k] += 1;
+        tally[2 * k + 1] += ok;
+    }
+    keep[2 * k] = ok;
+    keep[2 * k + 1] = 0;
+    maxsq[k] = 0ull;
+    jmax[k] = 0u;
 }
 
 __global__ void k_hist_count(int* valid) { *valid = min(*valid + 1, 2); }
@@ -765,6 +887,8 @@ int tb_mixed_setup(tb_ctx* c) {
     TB_CUDA(cudaMemset(m->hvalid, 0, 4 * sizeof(int)));
     TB_CUDA(cudaMalloc(&m->iter, sizeof(int)));
     TB_CUDA(cudaMemset(m->iter, 0, sizeof(int)));
+    TB_CUDA(cudaMalloc(&m->lkeep, 2 * K * sizeof(int)));
+    TB_CUDA(cudaMemset(m->lkeep, 0, 2 * K * sizeof(int)));
     if (c->cfg.warm_start)
         for (auto& h : m->hist)
             for (cplx*& p : h) TB_CUDA(cudaMalloc(&p, tb_n3(c) * sizeof(cplx)));
@@ -830,6 +954,7 @@ void tb_mixed_invalidate(tb_ctx* c) {
     Mixed* m = get(c);
     if (!m) return;
     for (int& t : m->last_t) t = -9;
+    for (int& v : m->hv_host) v = 0;
 }
 
 int tb_mixed_graph_pre(tb_ctx* c, int t, cudaStream_t s) {
@@ -842,8 +967,11 @@ int tb_mixed_graph_pre(tb_ctx* c, int t, cudaStream_t s) {
 
 void tb_mixed_graph_post(tb_ctx* c, int t) {
     Mixed* m = get(c);
-    if (m && c->cfg.warm_start)
-        for (int& q : m->last_t) q = t;
+    if (!m || !c->cfg.warm_start) return;
+    for (int q = 0; q < 4; q++) {
+        m->hv_host[q] = m->last_t[q] == t - 1 ? std::min(m->hv_host[q] + 1, 2) : 1;
+        m->last_t[q] = t;
+    }
 }
 
 void tb_mixed_free(tb_ctx* c) {
@@ -853,7 +981,7 @@ void tb_mixed_free(tb_ctx* c) {
         for (cplx* p : h)
             if (p) cudaFree(p);
     for (void* p : {(void*)m->e, (void*)m->r, (void*)m->rr, (void*)m->tab, (void*)m->coef, (void*)m->qdy2, (void*)m->ainv,
-                    (void*)m->maxsq, (void*)m->hvalid, (void*)m->iter})
+                    (void*)m->maxsq, (void*)m->hvalid, (void*)m->iter, (void*)m->lkeep})
         if (p) cudaFree(p);
     delete m;
     c->mixed = nullptr;
@@ -925,6 +1053,76 @@ static int record_loop(tb_ctx* c, const MgDev& M, double erro) {
     return TB_OK;
 }
 
+// 1 / |diagonal| of the fine y-line operator per mode and row, and the share
+// of k^2 beta^2 in it (rows j >= 1; the wall row is Dirichlet: 0).
+int tb_mixed_line_diag(tb_ctx* c, std::vector<float>& invD, std::vector<float>& mfeat) {
+    const int K = c->g.K, ny = c->g.ny;
+    invD.assign((size_t)K * ny, 0.f);
+    mfeat.assign((size_t)K * ny, 0.f);
+    std::vector<double> a, a0;
+    tb_poisson_band_matrix_dx(c, 0, 1, 1, c->h_dx2[0], a0);
+    for (int k = 0; k < K; k++) {
+        tb_poisson_band_matrix_dx(c, 0, 1, k + 1, c->h_dx2[0], a);
+        const int n = (int)(a.size() / 5);
+        if (n != ny) { tb_set_error("line operator has %d rows, expected %d", n, ny); return TB_ERR_STATE; }
+        for (int j = 1; j < ny; j++) {
+            const double d = a[(size_t)j + (size_t)n * 2], d0 = a0[(size_t)j + (size_t)n * 2];
+            if (d != 0.0) {
+                invD[(size_t)k * ny + j] = (float)(1.0 / std::fabs(d));
+                mfeat[(size_t)k * ny + j] = (float)(std::fabs(d - d0) / std::fabs(d));
+            }
+        }
+    }
+    return TB_OK;
+}
+
+// The learned first correction of stage ws's solve, before the loop: the
+// FP64 defect d0 of the extrapolated guess, the network's inputs (which also
+// shift the stage's history), then (when applying the network) its candidate
+// correction, kept per mode where max|d0 - L e| < max|d0|.  While sampling,
+// the guess is kept for the training targets.
+static int learned_first(tb_ctx* c, const MgDev& M, int ws, LearnSolve* L) {
+    Mixed* m = get(c);
+    const int K = c->g.K, nx = c->g.nx, ny = c->g.ny;
+    int r;
+    if ((r = tb_poisson_defect_f32(c, m->r, m->e, m->elems, m->maxsq))) return r;
+    TB_CUDA(cudaMemsetAsync(L->scl, 0, 3 * K * sizeof(float), c->stream));
+    const int* valid = m->hvalid + ws;
+    cplx *h0 = m->hist[ws][0], *h1 = m->hist[ws][1];
+    const unsigned nb = std::min<unsigned>(tb_blocks((size_t)nx * ny, 256), 64);
+    k_learn_scale<<<dim3(nb, K), 256, 0, c->stream>>>(M, h0, h1, valid, reinterpret_cast<unsigned*>(L->scl), L->invD, nx);
+    TB_CHECK_LAUNCH(c);
+    k_learn_prep<<<dim3(tb_blocks(nx, 32), tb_blocks(ny, 32), K), dim3(32, 8), 0, c->stream>>>(M, h0, h1, valid, L->scl,
+                                                                                             L->invD, L->mfeat, L->X, nx);
+    TB_CHECK_LAUNCH(c);
+    if (L->sample) {
+        const size_t pitch = c->g.lvl_elems * sizeof(cplx);
+        TB_CUDA(cudaMemcpy2DAsync(L->g0, pitch, c->pfc, pitch, (size_t)nx * ny * sizeof(cplx), K, cudaMemcpyDeviceToDevice,
+                                  c->stream));
+    }
+    if (!L->infer) {
+        TB_CUDA(cudaMemsetAsync(m->maxsq, 0, K * sizeof(unsigned long long), c->stream));
+        return TB_OK;
+    }
+    if ((r = tb_learn_run_net(c))) return r;
+    const size_t per = (size_t)(nx - 2) * (ny - 1);
+    k_learn_emit<<<tb_blocks(per * K, 256), 256, 0, c->stream>>>(M, L->out, L->scl, valid, nx);
+    TB_CHECK_LAUNCH(c);
+    k_resid<<<tb_blocks(per * K, 256), 256, 0, c->stream>>>(M, 0);
+    TB_CHECK_LAUNCH(c);
+    const unsigned nj = std::min<unsigned>(tb_blocks(per, 256), 64);
+    k_learn_judge<<<dim3(nj, K), 256, 0, c->stream>>>(M, L->jmax, valid, nx);
+    TB_CHECK_LAUNCH(c);
+    k_learn_keep<<<tb_blocks(K, 64), 64, 0, c->stream>>>(m->maxsq, L->jmax, m->lkeep, L->tally, valid, K);
+    TB_CHECK_LAUNCH(c);
+    MgDev Mk = M;
+    Mk.state = m->lkeep;
+    dim3 tgrid(tb_blocks(nx, 32), tb_blocks(ny, 32), K), tblk(32, 8);
+    k_apply<<<tgrid, tblk, 0, c->stream>>>(Mk, c->pfc, c->g.lvl_elems, nx, ny);
+    TB_CHECK_LAUNCH(c);
+    return TB_OK;
+}
+
 // One solve's per-mode state (hs: active flag and corrections, per mode)
 // and final defect (he) into the statistics.
 int tb_mixed_absorb_stats(tb_ctx* c, const int* hs, const double* he) {
@@ -957,13 +1155,19 @@ int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
     if ((r = tb_prof_begin(c, PROF_POISSON, &pall))) return r;
     if ((r = tb_poisson_begin(c, dwzdx))) return r;
     const int ws = (c->cfg.warm_start && c->ws_stage >= 1 && c->ws_stage <= 4) ? c->ws_stage - 1 : -1;
+    LearnSolve* L = ws >= 0 ? tb_learn_solve(c) : nullptr;
+    int hv = 0;   // usable history entries, known to the host in host-launched solves
     if (ws >= 0) {
         // a recorded step checks the continuity of its steps before each replay
-        if (!c->capturing && mx->last_t[ws] != c->ws_t - 1)
+        if (!c->capturing && mx->last_t[ws] != c->ws_t - 1) {
             TB_CUDA(cudaMemsetAsync(mx->hvalid + ws, 0, sizeof(int), c->stream));
+            mx->hv_host[ws] = 0;
+        }
+        hv = mx->hv_host[ws];
         k_extrap<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(c->pfc, c->g.lvl_elems, mx->hist[ws][0],
-                                                                  mx->hist[ws][1], mx->hvalid + ws, nx, ny, K);
+                                                                  mx->hist[ws][1], mx->hvalid + ws, nx, ny, K, L ? 0 : 1);
         TB_CHECK_LAUNCH(c);
+        if (L && (r = learned_first(c, M, ws, L))) return r;
     }
     if (c->capturing) {
         if ((r = record_loop(c, M, erro))) return r;
@@ -987,12 +1191,16 @@ int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
             TB_CHECK_LAUNCH(c);
         }
     }
+    if (L && L->sample && !c->capturing && hv >= 2 && (r = tb_learn_collect(c))) return r;
     if ((r = tb_poisson_end(c))) return r;
     if (ws >= 0) {   // this solve becomes the newest entry of the stage's history
         TB_CUDA(cudaMemcpyAsync(mx->hist[ws][0], c->uy, tb_n3(c) * sizeof(cplx), cudaMemcpyDeviceToDevice, c->stream));
         k_hist_count<<<1, 1, 0, c->stream>>>(mx->hvalid + ws);
         TB_CHECK_LAUNCH(c);
-        if (!c->capturing) mx->last_t[ws] = c->ws_t;
+        if (!c->capturing) {
+            mx->last_t[ws] = c->ws_t;
+            mx->hv_host[ws] = std::min(hv + 1, 2);
+        }
     }
     if ((r = tb_prof_end(c, PROF_POISSON, pall))) return r;
     if (c->capturing) {   // the step's statistics are read after each replay
