@@ -199,13 +199,28 @@ int tb_learn_enable(tb_ctx* ctx, int on);       /* apply the network in every so
 /* Collect crops_per_solve crops from every solve into a buffer of `capacity`
    crops; capacity 0 stops collecting and keeps the crops for training.     */
 int tb_learn_sample(tb_ctx* ctx, long long capacity, int crops_per_solve, unsigned long long seed);
-int tb_learn_train(tb_ctx* ctx, int iters, int batch, float lr, unsigned long long seed, double* loss);
+/* Adam on crops 0 .. n_train-1 (all when n_train <= 0); the first run from
+   fresh weights sets the input and output scales from those crops.          */
+int tb_learn_train(tb_ctx* ctx, long long n_train, int iters, int batch, float lr, unsigned long long seed,
+                   double* loss);
+/* Defect loss of the network over crops first .. first+n-1 and that of a
+   zero correction (the defect the extrapolated guess leaves).             */
+int tb_learn_eval(tb_ctx* ctx, long long first, long long n, double* mse, double* target_ms);
 int tb_learn_get_stats(tb_ctx* ctx, tb_learn_stats* st);
-/* The training kernels on caller data (host memory, current device):
-   loss and gradient over n crops (n, 5, 72, 72), planes 0-3 the inputs and
-   plane 4 the target; and the network's output on n images (n, 4, H, W).  */
-int tb_learn_grad(const float* w, const float* crops, int n, double* loss, float* grad);
+/* Copy collected crops first .. first+n-1, each (5, 72, 72) floats.       */
+int tb_learn_get_samples(tb_ctx* ctx, long long first, long long n, float* dst);
+/* The training kernels on caller data (host memory): loss and gradient over
+   n crops (n, 5, 72, 72), planes 0-3 the inputs and plane 4 the target,
+   with meta (n, 3) = image (2k + part), first row, first column on the
+   context's grid; and the network's output on n images (n, 4, H, W).
+   tb_learn_op_tables gives mode k's operator tables as the loss uses them
+   (den, ify, alpha^2, k^2 beta^2, w_k, 24 coefficients, qdy2(ny), 1/|D|(ny));
+   tb_learn_op_apply gives -L e of mode k through the solver's own residual
+   kernel (e, out: (nx, ny), y fastest).                                   */
+int tb_learn_grad(tb_ctx* ctx, const float* w, const float* crops, const int* meta, int n, double* loss, float* grad);
 int tb_learn_forward(const float* w, const float* x, int n, int H, int W, float* out);
+int tb_learn_op_tables(tb_ctx* ctx, int k, float* tab);
+int tb_learn_op_apply(tb_ctx* ctx, int k, const float* e, float* out);
 
 /* ---- ensembles: independent runs advanced together --------------------
    One recorded CUDA graph advances every member by one step: the members'

@@ -124,9 +124,13 @@ def load():
     lib.tb_learn_get_weights.argtypes = [P, F]
     lib.tb_learn_enable.argtypes = [P, C.c_int]
     lib.tb_learn_sample.argtypes = [P, C.c_longlong, C.c_int, C.c_ulonglong]
-    lib.tb_learn_train.argtypes = [P, C.c_int, C.c_int, C.c_float, C.c_ulonglong, D]
+    lib.tb_learn_train.argtypes = [P, C.c_longlong, C.c_int, C.c_int, C.c_float, C.c_ulonglong, D]
+    lib.tb_learn_eval.argtypes = [P, C.c_longlong, C.c_longlong, D, D]
     lib.tb_learn_get_stats.argtypes = [P, C.POINTER(LearnStats)]
-    lib.tb_learn_grad.argtypes = [F, F, C.c_int, D, F]
+    lib.tb_learn_get_samples.argtypes = [P, C.c_longlong, C.c_longlong, F]
+    lib.tb_learn_grad.argtypes = [P, F, F, C.POINTER(C.c_int), C.c_int, D, F]
+    lib.tb_learn_op_tables.argtypes = [P, C.c_int, F]
+    lib.tb_learn_op_apply.argtypes = [P, C.c_int, F, F]
     lib.tb_learn_forward.argtypes = [F, F, C.c_int, C.c_int, C.c_int, F]
     lib.tb_ensemble_create.argtypes = [C.POINTER(P), C.c_int, C.POINTER(P)]
     lib.tb_ensemble_step.argtypes = [P, C.POINTER(C.c_int)]
@@ -169,17 +173,6 @@ def learn_param_count():
 
 def learn_crop_size():
     return int(load().tb_learn_crop_size())
-
-
-def learn_grad(w, crops):
-    """Loss and gradient of the learned-correction network on crops
-    (n, 5, 72, 72) float32, computed by the library's training kernels."""
-    w = np.ascontiguousarray(w, dtype=np.float32)
-    crops = np.ascontiguousarray(crops, dtype=np.float32)
-    g = np.zeros(learn_param_count(), dtype=np.float32)
-    loss = np.zeros(1)
-    check(load().tb_learn_grad(fptr(w), fptr(crops), crops.shape[0], dptr(loss), fptr(g)), "tb_learn_grad")
-    return float(loss[0]), g
 
 
 def learn_forward(w, x):
@@ -353,10 +346,49 @@ class Context:
     def learn_sample(self, capacity, crops_per_solve=16, seed=1):
         self._c(self.lib.tb_learn_sample(self.h, int(capacity), int(crops_per_solve), seed), "tb_learn_sample")
 
-    def learn_train(self, iters, batch=32, lr=1e-3, seed=1):
+    def learn_train(self, iters, batch=32, lr=1e-3, seed=1, n_train=0):
+        """Adam on the first n_train crops (all when 0); returns the mean batch
+        loss over the last tenth of the iterations."""
         loss = np.zeros(1)
-        self._c(self.lib.tb_learn_train(self.h, int(iters), int(batch), float(lr), seed, dptr(loss)), "tb_learn_train")
+        self._c(self.lib.tb_learn_train(self.h, int(n_train), int(iters), int(batch), float(lr), seed, dptr(loss)),
+                "tb_learn_train")
         return float(loss[0])
+
+    def learn_eval(self, first, n):
+        """(mean squared error, mean squared target) over crops first .. first+n-1."""
+        a, b = np.zeros(1), np.zeros(1)
+        self._c(self.lib.tb_learn_eval(self.h, int(first), int(n), dptr(a), dptr(b)), "tb_learn_eval")
+        return float(a[0]), float(b[0])
+
+    def learn_samples(self, first, n):
+        cw = learn_crop_size()
+        out = np.zeros((int(n), 5, cw, cw), dtype=np.float32)
+        self._c(self.lib.tb_learn_get_samples(self.h, int(first), int(n), fptr(out)), "tb_learn_get_samples")
+        return out
+
+    def learn_grad(self, w, crops, meta):
+        """Defect loss and gradient of the network on crops (n, 5, 72, 72) with
+        meta (n, 3), by the library's training kernels on this grid."""
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        crops = np.ascontiguousarray(crops, dtype=np.float32)
+        meta = np.ascontiguousarray(meta, dtype=np.int32)
+        g = np.zeros(learn_param_count(), dtype=np.float32)
+        loss = np.zeros(1)
+        self._c(self.lib.tb_learn_grad(self.h, fptr(w), fptr(crops), meta.ctypes.data_as(C.POINTER(C.c_int)),
+                                       crops.shape[0], dptr(loss), fptr(g)), "tb_learn_grad")
+        return float(loss[0]), g
+
+    def learn_op_tables(self, k):
+        tab = np.zeros(29 + 2 * self.cfg.ny, dtype=np.float32)
+        self._c(self.lib.tb_learn_op_tables(self.h, int(k), fptr(tab)), "tb_learn_op_tables")
+        return tab
+
+    def learn_op_apply(self, k, e):
+        """-L e of mode k (e: (nx, ny) float32) by the solver's residual kernel."""
+        e = np.ascontiguousarray(e, dtype=np.float32)
+        out = np.zeros_like(e)
+        self._c(self.lib.tb_learn_op_apply(self.h, int(k), fptr(e), fptr(out)), "tb_learn_op_apply")
+        return out
 
     def learn_stats(self):
         st = LearnStats()

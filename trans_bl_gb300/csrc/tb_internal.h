@@ -208,6 +208,19 @@ struct LearnSolve {
     cplx* g0 = nullptr;          // guess before any correction (while sampling)
     long long* tally = nullptr;  // (K, 2) solves tried / corrections kept per mode
 };
+// The fine-level FP32 operator of the mixed form (the operator of k_resid at
+// level 0): device tables and scalars.
+struct FineOp {
+    const float* coef;     // sp(7) cp(8) pp(4) lp(5) of the finest level
+    const float* qdy2;     // (ny)
+    const double* k2b2;    // (K)
+    float den, ify, alpha2;
+    int nx, ny, K;
+};
+int tb_mixed_fine_op(tb_ctx* c, FineOp* op);
+// FP32 residual r - L e of the finest level for one mode (tests of the
+// learned correction's operator): host r, e and out in line-contiguous (nx, ny).
+int tb_mixed_resid_mode(tb_ctx* c, int k, const float* e, float* out);
 LearnSolve* tb_learn_solve(tb_ctx* c);     // null unless the learned form is on
 int tb_learn_run_net(tb_ctx* c);           // X -> out on c->stream
 int tb_learn_collect(tb_ctx* c);           // this solve's crops into the sample buffer

@@ -508,8 +508,9 @@ __global__ void k_learn_prep(MgDev M, const cplx* h0, cplx* h1, const int* valid
     }
     if (nv < 2) return;   // uniform over the block
     __syncthreads();
-    const float sv = scl[3 * k], si = scl[3 * k + 1], sd = scl[3 * k + 2];
-    const float iv = sv > 0.f ? 1.f / sv : 0.f, ii = si > 0.f ? 1.f / si : 0.f, id = sd > 0.f ? 1.f / sd : 0.f;
+    // one scale for the three field planes: s = max|v1 - v2|
+    const float si = scl[3 * k + 1];
+    const float ii = si > 0.f ? 1.f / si : 0.f, iv = ii, id = ii;
     float* Xr = X + (size_t)(2 * k) * 4 * per;   // planes of the real part, then of the imaginary part
     float* Xi = Xr + 4 * per;
     for (int r = threadIdx.y; r < 32; r += 8) {
@@ -1120,6 +1121,50 @@ static int learned_first(tb_ctx* c, const MgDev& M, int ws, LearnSolve* L) {
     dim3 tgrid(tb_blocks(nx, 32), tb_blocks(ny, 32), K), tblk(32, 8);
     k_apply<<<tgrid, tblk, 0, c->stream>>>(Mk, c->pfc, c->g.lvl_elems, nx, ny);
     TB_CHECK_LAUNCH(c);
+    return TB_OK;
+}
+
+int tb_mixed_fine_op(tb_ctx* c, FineOp* op) {
+    Mixed* m = get(c);
+    if (!m) { tb_set_error("mixed form not set up"); return TB_ERR_STATE; }
+    MgDev M = make(c);
+    op->coef = M.coef + 24 * M.ylvl[0];
+    op->qdy2 = M.qdy2 + (size_t)M.ny * M.ylvl[0];
+    op->k2b2 = M.k2b2;
+    op->den = M.qx[0];
+    op->ify = M.ify;
+    op->alpha2 = M.alpha2;
+    op->nx = m->ptsx[0];
+    op->ny = M.ny;
+    op->K = M.K;
+    return TB_OK;
+}
+
+// -L e on the finest level of mode k alone (r = 0), through k_resid.
+int tb_mixed_resid_mode(tb_ctx* c, int k, const float* e, float* out) {
+    Mixed* m = get(c);
+    if (!m) { tb_set_error("mixed form not set up"); return TB_ERR_STATE; }
+    const int K = c->g.K, nx = c->g.nx, ny = c->g.ny;
+    if (k < 0 || k >= K) { tb_set_error("mode out of range"); return TB_ERR_ARG; }
+    const size_t img = (size_t)nx * ny;
+    std::vector<float2> h(img);
+    for (size_t q = 0; q < img; q++) h[q] = make_float2(e[q], 0.f);
+    std::vector<int> st((size_t)2 * K, 0);
+    st[2 * k] = 1;
+    MgDev M = make(c);
+    TB_CUDA(cudaStreamSynchronize(c->stream));
+    TB_CUDA(cudaMemcpy(m->e + (size_t)k * m->elems, h.data(), img * sizeof(float2), cudaMemcpyHostToDevice));
+    TB_CUDA(cudaMemset(m->r + (size_t)k * m->elems, 0, img * sizeof(float2)));
+    TB_CUDA(cudaMemset(m->rr + (size_t)k * m->elems, 0, img * sizeof(float2)));
+    TB_CUDA(cudaMemcpy(m->lkeep, st.data(), st.size() * sizeof(int), cudaMemcpyHostToDevice));
+    M.state = m->lkeep;
+    const size_t per = (size_t)(nx - 2) * (ny - 1);
+    k_resid<<<tb_blocks(per * K, 256), 256, 0, c->stream>>>(M, 0);
+    TB_CHECK_LAUNCH(c);
+    TB_CUDA(cudaMemcpyAsync(h.data(), m->rr + (size_t)k * m->elems, img * sizeof(float2), cudaMemcpyDeviceToHost, c->stream));
+    TB_CUDA(cudaStreamSynchronize(c->stream));
+    for (size_t q = 0; q < img; q++) out[q] = h[q].x;
+    TB_CUDA(cudaMemset(m->e + (size_t)k * m->elems, 0, img * sizeof(float2)));
     return TB_OK;
 }
 
