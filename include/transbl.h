@@ -172,6 +172,15 @@ int tb_rk_stage(tb_ctx* ctx, int stage, int t);   /* stage 1..4 of step t       
 int tb_step(tb_ctx* ctx, int t);                  /* four stages                 */
 int tb_steps(tb_ctx* ctx, int t0, int nsteps);    /* t0 .. t0+nsteps-1           */
 int tb_get_poisson_stats(tb_ctx* ctx, tb_poisson_stats* st);
+/* Mixed form, P >= 16: the spanwise transforms of the disturbance products
+   in the nonlinear terms run as DFT-matrix GEMMs on the tensor cores
+   (split-BF16 operands, FP32 accumulation); 0 selects the FP32 FFT passes.
+   Default 1.                                                                */
+int tb_nl_tensor_cores(tb_ctx* ctx, int on);
+/* The DFT matrices of those GEMMs in double precision, P x P row-major:
+   forward 0: physical z from slot s (slots: Re c0 (unused), Im c0 as the
+   Nyquist term, Re and Im of modes 1 .. P/2-1); forward 1: slot from z.     */
+int tb_dft_matrix(int P, int forward, double* out);
 
 /* ---- learned first correction of the mixed v-Poisson solve ------------
    A convolutional network (four 3x3 layers, 4 -> 32 -> 32 -> 32 -> 1

@@ -119,6 +119,8 @@ def load():
     lib.tb_write_pert.argtypes = [P, C.c_char_p]
     lib.tb_io_set_subrecord_limit.argtypes = [C.c_longlong]
     F = C.POINTER(C.c_float)
+    lib.tb_nl_tensor_cores.argtypes = [P, C.c_int]
+    lib.tb_dft_matrix.argtypes = [C.c_int, C.c_int, D]
     lib.tb_learn_init.argtypes = [P, C.c_ulonglong]
     lib.tb_learn_set_weights.argtypes = [P, F]
     lib.tb_learn_get_weights.argtypes = [P, F]
@@ -165,6 +167,14 @@ def default_config(**kw):
 
 def fptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def dft_matrix(P, forward):
+    """The tensor-core passes' DFT matrix (P x P, double): forward False maps
+    slots to physical z, True physical z to slots."""
+    out = np.zeros((P, P))
+    check(load().tb_dft_matrix(int(P), 1 if forward else 0, dptr(out)), "tb_dft_matrix")
+    return out
 
 
 def learn_param_count():
@@ -324,6 +334,9 @@ class Context:
 
     def write_pert(self, path):
         self._c(self.lib.tb_write_pert(self.h, os.fsencode(path)), "tb_write_pert")
+
+    def nl_tensor_cores(self, on=True):
+        self._c(self.lib.tb_nl_tensor_cores(self.h, 1 if on else 0), "tb_nl_tensor_cores")
 
     # learned first correction ----------------------------------------------
     def learn_init(self, seed=1):

@@ -57,7 +57,7 @@ int down(tb_ctx* c, double* h, const cplx* d, size_t n) {
 int finish(tb_ctx* c) {
     TB_CUDA(cudaGetLastError());
     TB_CUDA(cudaStreamSynchronize(c->stream));
-    return TB_OK;
+    return tb_tc_check(c);
 }
 bool ready(tb_ctx* c) {
     if (!c) { tb_set_error("null context"); return false; }
@@ -107,6 +107,7 @@ int tb_create(const tb_config* cfg, tb_ctx** out) {
     c->dt2 = 0.5 * c->dt; c->dt6 = c->dt / 6.0;
     c->dz = (2.0 * PI) / ((double)g.P * cfg->beta);
     cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         tb_set_error("cudaStreamCreate failed: %s", cudaGetErrorString(cudaGetLastError()));
         delete c;
@@ -143,6 +144,8 @@ int tb_destroy(tb_ctx* c) {
     tb_graph_free(c);
     tb_learn_free(c);
     if (c->nl_phys) cudaFree(c->nl_phys);
+    if (c->dft_tc) cudaFree(c->dft_tc);
+    if (c->tc_err) cudaFree(c->tc_err);
     for (int q = 0; q < 24; q++) if (c->tmp[q]) cudaFree(c->tmp[q]);
     for (auto& r : c->prof_open) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : c->prof_pool) cudaEventDestroy(e);
@@ -264,6 +267,13 @@ int tb_steps(tb_ctx* c, int t0, int n) {
         int r = tb_step(c, t);
         if (r) return r;
     }
+    return TB_OK;
+}
+int tb_nl_tensor_cores(tb_ctx* c, int on) {
+    if (!c) { tb_set_error("null context"); return TB_ERR_ARG; }
+    TB_CUDA(cudaStreamSynchronize(c->stream));
+    c->nl_tensor = on != 0;
+    tb_graph_reset(c);
     return TB_OK;
 }
 int tb_get_poisson_stats(tb_ctx* c, tb_poisson_stats* st) {

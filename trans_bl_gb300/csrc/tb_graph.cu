@@ -168,6 +168,7 @@ int tb_graph_step(tb_ctx* c, int t) {
     TB_CUDA(cudaMemcpyAsync(he.data(), c->gerr, he.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     TB_CUDA(cudaStreamSynchronize(c->stream));
     tb_mixed_graph_post(c, t);
+    if ((r = tb_tc_check(c))) return r;
     return tb_graph_post(c, hs.data(), he.data());
 }
 
@@ -296,6 +297,8 @@ int tb_ensemble_step(tb_ensemble* e, const int* t) {
     TB_CUDA(cudaStreamSynchronize(e->s));
     int rc = TB_OK;
     for (size_t i = 0; i < e->m.size(); i++) {
+        r = tb_tc_check(e->m[i]);
+        if (r && !rc) rc = r;
         tb_mixed_graph_post(e->m[i], t[i]);
         r = tb_graph_post(e->m[i], e->hs[i].data(), e->he[i].data());
         if (r && !rc) rc = r;

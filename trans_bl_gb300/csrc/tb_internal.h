@@ -137,6 +137,11 @@ struct tb_ctx {
     int g_stage = 0;                       // stage being recorded (1..4)
     long long graph_gen = 0;               // bumped whenever recorded graphs go stale
     void* learn = nullptr;                 // learned first correction (tb_learn.cu)
+    // spanwise transforms of the mixed nonlinear terms on the tensor cores
+    int nl_tensor = 1;                     // 0: the FP32 FFT passes instead
+    uint16_t* dft_tc = nullptr;            // BF16 DFT matrices (inverse hi, lo; forward hi, lo)
+    int* tc_err = nullptr;                 // set when a bounded MMA wait ran out
+    int sm_count = 0;
 };
 
 // Kernel families timed by tb_profile (index into prof_ms / prof_n).
@@ -229,6 +234,8 @@ int tb_mixed_line_diag(tb_ctx* c, std::vector<float>& invD, std::vector<float>& 
 
 // Step graph support (tb_graph.cu, tb_mixed.cu, tb_spectral.cu)
 int tb_spectral_prepare(tb_ctx* c);               // lazy tables/buffers of the step, made before a capture
+int tb_tc_check(tb_ctx* c);                       // error of the tensor-core passes since the last check
+void tb_dft_matrices(int P, std::vector<uint16_t>& out);
 int tb_mixed_graph_pre(tb_ctx* c, int t, cudaStream_t s);   // warm-start continuity before a replay of step t
 void tb_mixed_graph_post(tb_ctx* c, int t);       // after it
 int tb_mixed_absorb_stats(tb_ctx* c, const int* hs, const double* he);   // one solve's pstate/perr into stats

@@ -11,6 +11,10 @@
 // twiddles from a constant table instead of the reference's rotation
 // recurrence.
 #include "tb_internal.h"
+#include "tb_tc.cuh"
+#include <cuda_bf16.h>
+#include <cstring>
+#include <algorithm>
 #include <cmath>
 
 #define TW_N 512
@@ -289,6 +293,236 @@ __global__ void __launch_bounds__(128) k_nl_four(NlArgs A, const float* __restri
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same two passes on the tensor cores: the spanwise transforms of the
+// disturbance as dense DFT-matrix GEMMs (tcgen05.mma, kind::f16), operands
+// split into BF16 high and low parts, a b ~ ah bh + ah bl + al bh,
+// accumulated in FP32 in tensor memory.  A tile is 128 points (one per
+// thread and tensor-memory lane); per point the P "slots" hold Re c0 (0: the
+// mean stays in FP64), Im c0 (the packed Nyquist term) and Re, Im of modes
+// 1 .. P/2-1.  Pass 1: phys[pt][z] = sum_s slot[pt][s] Tinv[z][s]; pass 2:
+// slot[pt][s] = sum_z prod[pt][z] Tfwd[s][z], the transforms to_phys_dist and
+// to_four_f above written as matrices (tb_dft_matrices).
+//
+// Shared memory, K-major without swizzle: element (row r, k) of an operand
+// with R rows sits at (k / 8) * (R * 16) + r * 16 + (k % 8) * 2 bytes, so a
+// core matrix (8 rows x 8 k) is 128 contiguous bytes, core matrices
+// adjacent in rows are 128 bytes apart and those adjacent in k R * 16 apart.
+template <int P>
+struct TcLayout {
+    static constexpr int AB = 128 * P * 2, BB = P * P * 2;                 // bytes of one operand part
+    static constexpr int A_HI = 0, A_LO = AB, B_HI = 2 * AB, B_LO = 2 * AB + BB;
+    // reach of a descriptor under either reading of its two offsets, so every
+    // address an MMA can form stays inside the allocation
+    static constexpr int EXT_A = (P / 8 - 2) * 2048 + 15 * 2048 + 256;
+    static constexpr int EXT_B = (P / 8 - 2) * P * 16 + (P / 8 - 1) * P * 16 + 256;
+    static constexpr int TAIL0 = (A_LO + EXT_A > B_LO + EXT_B) ? A_LO + EXT_A : B_LO + EXT_B;
+    static constexpr int BAR = ((TAIL0 > B_LO + BB ? TAIL0 : B_LO + BB) + 15) / 16 * 16;
+    static constexpr int BYTES = BAR + 16;
+    static constexpr uint32_t NCOL = P < 32 ? 32 : P;                      // tensor-memory columns
+    static constexpr uint32_t ID = tbtc::idesc_bf16_f32(128, P);
+};
+
+__device__ __forceinline__ void split_bf16(float x, unsigned short& h, unsigned short& l) {
+    const __nv_bfloat16 hb = __float2bfloat16_rn(x);
+    const __nv_bfloat16 lb = __float2bfloat16_rn(x - __bfloat162float(hb));
+    h = __bfloat16_as_ushort(hb);
+    l = __bfloat16_as_ushort(lb);
+}
+
+// Row `row` of the A operand (P values) into its high and low parts.
+template <int P>
+__device__ __forceinline__ void stage_row(unsigned char* sm, int row, const float* v) {
+    using Lt = TcLayout<P>;
+#pragma unroll
+    for (int g = 0; g < P / 8; g++) {
+        unsigned short h[8], l[8];
+#pragma unroll
+        for (int e = 0; e < 8; e++) split_bf16(v[8 * g + e], h[e], l[e]);
+        uint4 H, L;
+        H.x = h[0] | ((uint32_t)h[1] << 16); H.y = h[2] | ((uint32_t)h[3] << 16);
+        H.z = h[4] | ((uint32_t)h[5] << 16); H.w = h[6] | ((uint32_t)h[7] << 16);
+        L.x = l[0] | ((uint32_t)l[1] << 16); L.y = l[2] | ((uint32_t)l[3] << 16);
+        L.z = l[4] | ((uint32_t)l[5] << 16); L.w = l[6] | ((uint32_t)l[7] << 16);
+        *reinterpret_cast<uint4*>(sm + Lt::A_HI + g * 2048 + row * 16) = H;
+        *reinterpret_cast<uint4*>(sm + Lt::A_LO + g * 2048 + row * 16) = L;
+    }
+}
+
+// One thread issues the tile's MMAs (3 per 16-wide k-step) and commits them.
+template <int P>
+__device__ __forceinline__ void tile_mma(unsigned char* sm, uint32_t tmem, uint64_t* bar) {
+    using Lt = TcLayout<P>;
+    const uint32_t base = tbtc::smem_u32(sm);
+#pragma unroll
+    for (int ks = 0; ks < P / 16; ks++) {
+        const uint32_t ao = ks * 2 * 2048, bo = ks * 2 * P * 16;
+        const uint64_t ah = tbtc::sdesc(base + Lt::A_HI + ao, 2048, 128), al = tbtc::sdesc(base + Lt::A_LO + ao, 2048, 128);
+        const uint64_t bh = tbtc::sdesc(base + Lt::B_HI + bo, P * 16, 128), bl = tbtc::sdesc(base + Lt::B_LO + bo, P * 16, 128);
+        tbtc::mma_bf16(tmem, ah, bh, Lt::ID, ks > 0);
+        tbtc::mma_bf16(tmem, ah, bl, Lt::ID, 1);
+        tbtc::mma_bf16(tmem, al, bh, Lt::ID, 1);
+    }
+    tbtc::mma_commit(bar);
+}
+
+// Set-up shared by both passes: the constant B operand (high, low) into
+// shared memory, the mbarrier, and the tensor-memory columns.
+template <int P>
+__device__ __forceinline__ uint32_t tc_setup(unsigned char* sm, const uint16_t* mats) {
+    using Lt = TcLayout<P>;
+    const int t = threadIdx.x;
+    for (int i = t; i < P * P / 8; i += blockDim.x) {
+        reinterpret_cast<uint4*>(sm + Lt::B_HI)[i] = reinterpret_cast<const uint4*>(mats)[i];
+        reinterpret_cast<uint4*>(sm + Lt::B_LO)[i] = reinterpret_cast<const uint4*>(mats + P * P)[i];
+    }
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + Lt::BAR);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(sm + Lt::BAR + 8);
+    if (t == 0) tbtc::mbar_init(bar, 1);
+    if ((t >> 5) == 0) {
+        tbtc::tmem_alloc(slot, Lt::NCOL);
+        tbtc::tmem_relinquish();
+    }
+    tbtc::fence_before_sync();
+    __syncthreads();
+    tbtc::fence_after_sync();
+    return *slot;
+}
+
+// Issue, wait (bounded) and read: returns false (for the whole block) when
+// the wait ran out, after which the caller stops issuing.
+template <int P>
+__device__ __forceinline__ bool tc_run(unsigned char* sm, uint32_t tmem, uint32_t& phase) {
+    using Lt = TcLayout<P>;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + Lt::BAR);
+    tbtc::fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tbtc::fence_after_sync();
+        tile_mma<P>(sm, tmem, bar);
+    }
+    const bool ok = tbtc::mbar_wait(bar, phase);
+    tbtc::fence_after_sync();
+    const bool all = !__syncthreads_or(!ok);
+    if (all) phase ^= 1u;   // on a time-out `phase` stays that of the tile in flight
+    return all;
+}
+
+template <int P>
+__device__ __forceinline__ void tc_teardown(unsigned char* sm, uint32_t tmem, bool ok, uint32_t phase, int* err) {
+    using Lt = TcLayout<P>;
+    if (!ok) {   // let the MMAs of the abandoned tile finish (bounded) before freeing their columns
+        (void)tbtc::mbar_wait(reinterpret_cast<uint64_t*>(sm + Lt::BAR), phase);
+        if (threadIdx.x == 0) atomicExch(err, 1);
+    }
+    tbtc::fence_before_sync();
+    __syncthreads();
+    tbtc::fence_after_sync();
+    if ((threadIdx.x >> 5) == 0) tbtc::tmem_dealloc(tmem, Lt::NCOL);
+}
+
+__device__ __forceinline__ const cplx* nl_field(const NlArgs& A, int f) {
+    return (f == 0) ? A.ux : (f == 1) ? A.uy : (f == 2) ? A.uz : (f == 3) ? A.wx : (f == 4) ? A.wy : A.wz;
+}
+
+// Pass 1 on the tensor cores: tile = (field f, 128 points) -> ph[(f P + z) n2 + q].
+template <int P>
+__global__ void __launch_bounds__(128) k_nl_phys_tc(NlArgs A, float* __restrict__ ph, const uint16_t* __restrict__ mats,
+                                                    int* err) {
+    constexpr int N = P / 2;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const uint32_t tmem = tc_setup<P>(sm, mats);
+    const int t = threadIdx.x, warp = t >> 5;
+    const size_t n2 = A.n2;
+    const int tpf = (int)((n2 + 127) / 128), ntiles = 6 * tpf;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int f = tile / tpf;
+        const size_t q = (size_t)(tile % tpf) * 128 + t;
+        const cplx* F = nl_field(A, f);
+        float v[P];
+        v[0] = 0.f;
+        v[1] = q < n2 ? (float)F[q].y : 0.f;
+#pragma unroll
+        for (int k = 1; k < N; k++) {
+            cplx c = make_double2(0.0, 0.0);
+            if (k < A.K && q < n2) c = F[(size_t)k * n2 + q];
+            v[2 * k] = (float)c.x;
+            v[2 * k + 1] = (float)c.y;
+        }
+        stage_row<P>(sm, t, v);
+        if (!(ok = tc_run<P>(sm, tmem, phase))) break;
+#pragma unroll
+        for (int c0 = 0; c0 < P; c0 += 16) {
+            float w[16];
+            tbtc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, w);
+            if (q < n2) {
+#pragma unroll
+                for (int i = 0; i < 16; i++) ph[((size_t)f * P + c0 + i) * n2 + q] = w[i];
+            }
+        }
+        tbtc::fence_before_sync();
+        __syncthreads();
+    }
+    tc_teardown<P>(sm, tmem, ok, phase, err);
+}
+
+// Pass 2 on the tensor cores: tile = (output o, 128 points); the quadratic
+// disturbance term's slots plus the FP64 mean terms, as k_nl_four.
+template <int P>
+__global__ void __launch_bounds__(128) k_nl_four_tc(NlArgs A, const float* __restrict__ ph,
+                                                    const uint16_t* __restrict__ mats, int* err) {
+    constexpr int N = P / 2;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const uint32_t tmem = tc_setup<P>(sm, mats);
+    const int t = threadIdx.x, warp = t >> 5;
+    const size_t n2 = A.n2;
+    const int tpf = (int)((n2 + 127) / 128), ntiles = 3 * tpf;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int o = tile / tpf;
+        const size_t q = (size_t)(tile % tpf) * 128 + t;
+        const int p1 = (o == 0) ? 1 : (o == 1) ? 0 : 2, q1 = (o == 0) ? 3 : (o == 1) ? 5 : 4;
+        const int p2 = (o == 0) ? 0 : (o == 1) ? 2 : 1, q2 = (o == 0) ? 4 : (o == 1) ? 3 : 5;
+        float v[P];
+#pragma unroll
+        for (int z = 0; z < P; z++) v[z] = 0.f;
+        if (q < n2) {
+            const float *a1 = ph + (size_t)p1 * P * n2 + q, *b1 = ph + (size_t)q1 * P * n2 + q;
+            const float *a2 = ph + (size_t)p2 * P * n2 + q, *b2 = ph + (size_t)q2 * P * n2 + q;
+#pragma unroll
+            for (int z = 0; z < P; z++) {
+                const size_t zz = (size_t)z * n2;
+                v[z] = a1[zz] * b1[zz] - a2[zz] * b2[zz];
+            }
+        }
+        stage_row<P>(sm, t, v);
+        if (!(ok = tc_run<P>(sm, tmem, phase))) break;
+#pragma unroll
+        for (int c0 = 0; c0 < P; c0 += 16) tbtc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v + c0);
+        if (q < n2) {
+            const cplx *P1 = nl_field(A, p1) + q, *Q1 = nl_field(A, q1) + q, *P2 = nl_field(A, p2) + q, *Q2 = nl_field(A, q2) + q;
+            const double m1 = P1[0].x, n1 = Q1[0].x, m2 = P2[0].x, n2v = Q2[0].x;
+            cplx* out = ((o == 0) ? A.a : (o == 1) ? A.b : A.c) + q;
+            out[0] = make_double2(zap(m1 * n1 - m2 * n2v + (double)v[0]), 0.0);
+#pragma unroll
+            for (int k = 1; k < N; k++) {
+                if (k >= A.K) continue;
+                const size_t kk = (size_t)k * n2;
+                const cplx aq1 = Q1[kk], ap1 = P1[kk], aq2 = Q2[kk], ap2 = P2[kk];
+                const double vr = m1 * aq1.x + n1 * ap1.x - m2 * aq2.x - n2v * ap2.x + (double)v[2 * k];
+                const double vi = m1 * aq1.y + n1 * ap1.y - m2 * aq2.y - n2v * ap2.y + (double)v[2 * k + 1];
+                out[kk] = make_double2(zap(vr), zap(vi));
+            }
+        }
+        tbtc::fence_before_sync();
+        __syncthreads();
+    }
+    tc_teardown<P>(sm, tmem, ok, phase, err);
+}
+
 // Smagorinsky eddy viscosity and force nu_t lap(u) (les_par.f:6-211).
 struct LesArgs {
     const cplx *dudx, *dvdx, *dwdx, *dudy, *dvdy, *dwdy;   // Fourier gradients
@@ -492,11 +726,169 @@ int tb_launch_p_to_f(tb_ctx* c, cplx* four, const double* phys) {
     TB_CHECK_LAUNCH(c);
     return TB_OK;
 }
+// ---- the DFT matrices of the tensor-core passes ------------------------------
+static uint16_t bf16_bits(float f) {   // round to nearest even
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+static float bf16_value(uint16_t h) {
+    uint32_t u = (uint32_t)h << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+// to_phys_dist and to_four_f in double precision on slot vectors, with the
+// length-N complex transforms of cfft written as plain sums.
+static const double TB_PI = 3.14159265358979323846;
+static void host_cdft(int N, int sign, std::vector<double>& re, std::vector<double>& im) {
+    std::vector<double> r(N, 0.0), i(N, 0.0);
+    for (int m = 0; m < N; m++)
+        for (int k = 0; k < N; k++) {
+            const double a = sign * 2.0 * TB_PI * (double)((long)k * m % N) / N;
+            r[m] += re[k] * std::cos(a) - im[k] * std::sin(a);
+            i[m] += re[k] * std::sin(a) + im[k] * std::cos(a);
+        }
+    re = r;
+    im = i;
+}
+static void host_phys_from_slots(int P, const double* s, double* p) {
+    const int N = P / 2;
+    std::vector<double> re(N), im(N);
+    re[0] = 0.5 * s[1];
+    im[0] = -0.5 * s[1];
+    for (int k = 1; k < N; k++) {
+        const double Ar = s[2 * k], Ai = s[2 * k + 1], Br = s[2 * (N - k)], Bi = -s[2 * (N - k) + 1];
+        const double sr = 0.5 * (Ar + Br), si = 0.5 * (Ai + Bi), dr = 0.5 * (Ar - Br), di = 0.5 * (Ai - Bi);
+        const double wr = std::cos(2.0 * TB_PI * k / P), wi = -std::sin(2.0 * TB_PI * k / P);
+        re[k] = sr - (wr * di + wi * dr);
+        im[k] = si + (wr * dr - wi * di);
+    }
+    host_cdft(N, -1, re, im);
+    for (int m = 0; m < N; m++) { p[2 * m] = re[m]; p[2 * m + 1] = im[m]; }
+}
+static void host_slots_from_phys(int P, const double* p, double* s) {
+    const int N = P / 2;
+    std::vector<double> re(N), im(N);
+    for (int m = 0; m < N; m++) { re[m] = p[2 * m]; im[m] = p[2 * m + 1]; }
+    host_cdft(N, +1, re, im);
+    s[0] = (re[0] + im[0]) / P;
+    s[1] = 0.0;
+    for (int k = 1; k < N; k++) {
+        const double Fr = re[k], Fi = im[k], Gr = re[N - k], Gi = -im[N - k];
+        const double Er = 0.5 * (Fr + Gr), Ei = 0.5 * (Fi + Gi), gr = Fr - Gr, gi = Fi - Gi;
+        const double Or = 0.5 * gi, Oi = -0.5 * gr;
+        const double vr = std::cos(2.0 * TB_PI * k / P), vi = std::sin(2.0 * TB_PI * k / P);
+        s[2 * k] = 2.0 / P * (Er + (vr * Or - vi * Oi));
+        s[2 * k + 1] = 2.0 / P * (Ei + (vr * Oi + vi * Or));
+    }
+}
+
+// B operands of both passes, high and low BF16 parts, in the K-major core
+// layout of TcLayout: inverse (n = z, k = slot) then forward (n = slot, k = z).
+void tb_dft_matrices(int P, std::vector<uint16_t>& out) {
+    std::vector<double> Tinv((size_t)P * P), Tfwd((size_t)P * P), e(P), v(P);
+    for (int s = 0; s < P; s++) {
+        std::fill(e.begin(), e.end(), 0.0);
+        e[s] = 1.0;
+        host_phys_from_slots(P, e.data(), v.data());
+        for (int z = 0; z < P; z++) Tinv[(size_t)z * P + s] = v[z];
+        host_slots_from_phys(P, e.data(), v.data());   // e as a physical unit vector at z = s
+        for (int q = 0; q < P; q++) Tfwd[(size_t)q * P + s] = v[q];
+    }
+    out.assign((size_t)4 * P * P, 0);
+    auto put = [&](int part, const std::vector<double>& T) {   // T[n][k]
+        for (int n = 0; n < P; n++)
+            for (int k = 0; k < P; k++) {
+                const float x = (float)T[(size_t)n * P + k];
+                const uint16_t h = bf16_bits(x), l = bf16_bits(x - bf16_value(h));
+                const size_t o = (size_t)(k / 8) * (P * 8) + (size_t)n * 8 + (k % 8);
+                out[(size_t)part * P * P + o] = h;
+                out[(size_t)(part + 1) * P * P + o] = l;
+            }
+    };
+    put(0, Tinv);
+    put(2, Tfwd);
+}
+
+// The two matrices in double precision, P x P row-major [n][k]: forward 0
+// gives Tinv[z][slot], forward 1 gives Tfwd[slot][z].
+extern "C" int tb_dft_matrix(int P, int forward, double* out) {
+    if (!out || P < 4 || (P & (P - 1))) { tb_set_error("P must be a power of two >= 4"); return TB_ERR_ARG; }
+    std::vector<double> e(P), v(P);
+    for (int s = 0; s < P; s++) {
+        std::fill(e.begin(), e.end(), 0.0);
+        e[s] = 1.0;
+        if (forward) {
+            host_slots_from_phys(P, e.data(), v.data());
+            for (int q = 0; q < P; q++) out[(size_t)q * P + s] = v[q];
+        } else {
+            host_phys_from_slots(P, e.data(), v.data());
+            for (int z = 0; z < P; z++) out[(size_t)z * P + s] = v[z];
+        }
+    }
+    return TB_OK;
+}
+
+static bool tc_form(const tb_ctx* c) {
+    const int P = c->g.P;
+    return c->cfg.precision == TB_FORM_MIXED && c->nl_tensor && (P == 16 || P == 32 || P == 64 || P == 128);
+}
+
+static bool g_tc_attr[64][4] = {{false}};
+
+template <int P>
+static int tc_attrs(int dev) {
+    const int slot = P == 16 ? 0 : P == 32 ? 1 : P == 64 ? 2 : 3;
+    if (dev >= 0 && dev < 64 && g_tc_attr[dev][slot]) return TB_OK;
+    TB_CUDA(cudaFuncSetAttribute(k_nl_phys_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcLayout<P>::BYTES));
+    TB_CUDA(cudaFuncSetAttribute(k_nl_four_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcLayout<P>::BYTES));
+    if (dev >= 0 && dev < 64) g_tc_attr[dev][slot] = true;
+    return TB_OK;
+}
+
+static int ensure_tc(tb_ctx* c) {
+    if (!tc_form(c)) return TB_OK;
+    int r;
+    switch (c->g.P) {
+        case 16: r = tc_attrs<16>(c->device); break;
+        case 32: r = tc_attrs<32>(c->device); break;
+        case 64: r = tc_attrs<64>(c->device); break;
+        default: r = tc_attrs<128>(c->device); break;
+    }
+    if (r) return r;
+    if (!c->dft_tc) {
+        std::vector<uint16_t> m;
+        tb_dft_matrices(c->g.P, m);
+        TB_CUDA(cudaMalloc(&c->dft_tc, m.size() * sizeof(uint16_t)));
+        TB_CUDA(cudaMemcpy(c->dft_tc, m.data(), m.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    }
+    if (!c->tc_err) {
+        TB_CUDA(cudaMalloc(&c->tc_err, sizeof(int)));
+        TB_CUDA(cudaMemset(c->tc_err, 0, sizeof(int)));
+    }
+    return TB_OK;
+}
+
 int tb_spectral_prepare(tb_ctx* c) {
     int r = ensure_twiddles(c);
     if (r) return r;
     if (c->cfg.precision == TB_FORM_MIXED && c->g.P >= 4 && !c->nl_phys)
         TB_CUDA(cudaMalloc(&c->nl_phys, (size_t)6 * c->g.P * tb_n2(c) * sizeof(float)));
+    return ensure_tc(c);
+}
+
+int tb_tc_check(tb_ctx* c) {
+    if (!c->tc_err) return TB_OK;
+    int e = 0;
+    TB_CUDA(cudaMemcpy(&e, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        TB_CUDA(cudaMemset(c->tc_err, 0, sizeof(int)));
+        tb_set_error("nlterms (tensor cores): a bounded wait for the MMAs ran out");
+        return TB_ERR_TIMEOUT;
+    }
     return TB_OK;
 }
 
@@ -506,7 +898,27 @@ int tb_launch_nlterms(tb_ctx* c, cplx* a, cplx* b, cplx* cc) {
     NlArgs A{c->ux, c->uy, c->uz, c->wx, c->wy, c->wz, a, b, cc, (int)tb_n2(c), c->g.K};
     cudaEvent_t ps = nullptr;
     if ((r = tb_prof_begin(c, PROF_NLTERMS, &ps))) return r;
-    if (c->cfg.precision == TB_FORM_MIXED && c->g.P >= 4) {
+    if (tc_form(c)) {
+        if (!c->capturing && (r = tb_spectral_prepare(c))) return r;
+        const int P = c->g.P, sms = c->sm_count > 0 ? c->sm_count : 148;
+        const size_t tiles = (A.n2 + 127) / 128;
+        const unsigned g1 = (unsigned)std::min<size_t>(6 * tiles, (size_t)3 * sms);
+        const unsigned g2 = (unsigned)std::min<size_t>(3 * tiles, (size_t)3 * sms);
+        switch (P) {
+#define TB_TC_CASE(PP)                                                                                        \
+    case PP:                                                                                                   \
+        k_nl_phys_tc<PP><<<g1, 128, TcLayout<PP>::BYTES, c->stream>>>(A, c->nl_phys, c->dft_tc, c->tc_err);        \
+        TB_CHECK_LAUNCH(c);                                                                                    \
+        k_nl_four_tc<PP><<<g2, 128, TcLayout<PP>::BYTES, c->stream>>>(A, c->nl_phys, c->dft_tc + 2 * PP * PP,      \
+                                                                      c->tc_err);                              \
+        break;
+            TB_TC_CASE(16)
+            TB_TC_CASE(32)
+            TB_TC_CASE(64)
+            TB_TC_CASE(128)
+#undef TB_TC_CASE
+        }
+    } else if (c->cfg.precision == TB_FORM_MIXED && c->g.P >= 4) {
         size_t need = (size_t)6 * c->g.P * A.n2;
         if (!c->nl_phys) TB_CUDA(cudaMalloc(&c->nl_phys, need * sizeof(float)));
         TB_DISPATCH_P(c->g.P, (k_nl_phys<PP><<<tb_blocks(6 * (size_t)A.n2, 128), 128, 0, c->stream>>>(A, c->nl_phys)));
