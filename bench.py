@@ -51,6 +51,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     p.add_argument("--no-ensemble", action="store_true", help="skip the 12-run ensemble measurement")
+    p.add_argument("--no-graph", action="store_true",
+                   help="launch every kernel from the host (same kernels; for profilers that cannot enter "
+                        "graphs with conditional nodes)")
     return p.parse_args()
 
 
@@ -274,6 +277,8 @@ def main():
     from trans_bl_gb300 import api, configs
     form = args.form
     cfg = workload(form)
+    if args.no_graph:
+        cfg.step_graph = 0
     coefs, base = configs.setup_inputs(cfg)
     ctx = api.Context(cfg, coefs, base)
     pts = cfg.nx * cfg.ny * cfg.kfour
@@ -340,6 +345,7 @@ def main():
             "data": "synthetic (Falkner-Skan base flow, generated coefficients, seeded TS forcing phases, "
                     "seeded smooth disturbance)",
             "config": {"workload": workload_name(cfg), "form": form, "replicas": world,
+                       "step": "replayed CUDA graph" if (cfg.step_graph and form == "mixed") else "host-launched kernels",
                        "l2": "inputs larger than L2: working set ~5 GB vs 129 MB L2",
                        "start": "disturbed state (1e-3) past the forcing ramp",
                        "iterations_per_mode_last_solve": float(np.mean(stats["vcycles"][:cfg.kfour]))},

@@ -312,15 +312,14 @@ template <int P>
 struct TcLayout {
     static constexpr int AB = 128 * P * 2, BB = P * P * 2;                 // bytes of one operand part
     static constexpr int A_HI = 0, A_LO = AB, B_HI = 2 * AB, B_LO = 2 * AB + BB;
-    // reach of a descriptor under either reading of its two offsets, so every
-    // address an MMA can form stays inside the allocation
-    static constexpr int EXT_A = (P / 8 - 2) * 2048 + 15 * 2048 + 256;
-    static constexpr int EXT_B = (P / 8 - 2) * P * 16 + (P / 8 - 1) * P * 16 + 256;
-    static constexpr int TAIL0 = (A_LO + EXT_A > B_LO + EXT_B) ? A_LO + EXT_A : B_LO + EXT_B;
-    static constexpr int BAR = ((TAIL0 > B_LO + BB ? TAIL0 : B_LO + BB) + 15) / 16 * 16;
+    static constexpr int BAR = B_LO + BB;                                  // mbarrier, then the TMEM address
     static constexpr int BYTES = BAR + 16;
     static constexpr uint32_t NCOL = P < 32 ? 32 : P;                      // tensor-memory columns
     static constexpr uint32_t ID = tbtc::idesc_bf16_f32(128, P);
+    // resident blocks per SM: shared memory (227 KB), tensor memory (512 columns), at most 8
+    static constexpr int PER_SM_SMEM = (227 * 1024) / BYTES, PER_SM_TMEM = 512 / (int)NCOL;
+    static constexpr int PER_SM0 = PER_SM_SMEM < PER_SM_TMEM ? PER_SM_SMEM : PER_SM_TMEM;
+    static constexpr int PER_SM = PER_SM0 < 8 ? PER_SM0 : 8;
 };
 
 __device__ __forceinline__ void split_bf16(float x, unsigned short& h, unsigned short& l) {
@@ -902,16 +901,17 @@ int tb_launch_nlterms(tb_ctx* c, cplx* a, cplx* b, cplx* cc) {
         if (!c->capturing && (r = tb_spectral_prepare(c))) return r;
         const int P = c->g.P, sms = c->sm_count > 0 ? c->sm_count : 148;
         const size_t tiles = (A.n2 + 127) / 128;
-        const unsigned g1 = (unsigned)std::min<size_t>(6 * tiles, (size_t)3 * sms);
-        const unsigned g2 = (unsigned)std::min<size_t>(3 * tiles, (size_t)3 * sms);
         switch (P) {
 #define TB_TC_CASE(PP)                                                                                        \
-    case PP:                                                                                                   \
+    case PP: {                                                                                                 \
+        const size_t cap = (size_t)TcLayout<PP>::PER_SM * sms;                                                 \
+        const unsigned g1 = (unsigned)std::min<size_t>(6 * tiles, cap), g2 = (unsigned)std::min<size_t>(3 * tiles, cap); \
         k_nl_phys_tc<PP><<<g1, 128, TcLayout<PP>::BYTES, c->stream>>>(A, c->nl_phys, c->dft_tc, c->tc_err);        \
         TB_CHECK_LAUNCH(c);                                                                                    \
         k_nl_four_tc<PP><<<g2, 128, TcLayout<PP>::BYTES, c->stream>>>(A, c->nl_phys, c->dft_tc + 2 * PP * PP,      \
                                                                       c->tc_err);                              \
-        break;
+        break;                                                                                                 \
+    }
             TB_TC_CASE(16)
             TB_TC_CASE(32)
             TB_TC_CASE(64)
