@@ -40,6 +40,8 @@ def build_library(verbose=False):
     srcs = sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "-I" + os.path.join(ROOT, "include")]
+    # extra flags, e.g. the multigrid's tuning macros: TB_NVCC_EXTRA="-DTB_MG_NU_PRE=3"
+    common += os.environ.get("TB_NVCC_EXTRA", "").split()
     jobs = []
     for s in srcs:
         obj = os.path.join(BUILD, s.rsplit(".", 1)[0] + ".o")

@@ -56,6 +56,10 @@ namespace {
 #endif
 constexpr int NU_PRE = TB_MG_NU_PRE, NU_POST = TB_MG_NU_POST, INNER_VCYCLES = TB_MG_INNER;
 constexpr int RELAX_THREADS = 128;   // 4 warps, one line each
+#ifndef TB_RELAX_MIN_BLOCKS
+#define TB_RELAX_MIN_BLOCKS 8
+#endif
+constexpr int RELAX_MIN_BLOCKS = TB_RELAX_MIN_BLOCKS;   // resident blocks per SM the register budget allows
 constexpr int MG_MAX = 16;           // levels of the FP32 hierarchy
 constexpr int DIRECT_MAX = 400;      // unknowns per mode below which coarsening stops
 constexpr int DIRECT_LIMIT = 2048;   // largest directly solved level accepted
@@ -119,7 +123,7 @@ __device__ __forceinline__ float2 xsum(const float2* E, int n, int i, int j, int
 // 32 row chunks (local recurrences, warp scan of precomputed 2x2 chunk
 // propagators, fix-up with precomputed homogeneous responses).
 template <int S>
-__global__ void __launch_bounds__(RELAX_THREADS) k_relax(MgDev M, int l, int first, int step, int nlines) {
+__global__ void __launch_bounds__(RELAX_THREADS, RELAX_MIN_BLOCKS) k_relax(MgDev M, int l, int first, int step, int nlines) {
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = blockIdx.x * (RELAX_THREADS / 32) + wib;
     const int k = gw / nlines;
