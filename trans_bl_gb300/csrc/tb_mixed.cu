@@ -43,7 +43,7 @@ namespace {
 // (until dx >= the largest y-spacing, so that y-coupling dominates at every
 // point of the coarser levels and y-line relaxation smooths everywhere).
 #ifndef TB_MG_NU_PRE
-#define TB_MG_NU_PRE 2
+#define TB_MG_NU_PRE 1
 #endif
 #ifndef TB_MG_NU_POST
 #define TB_MG_NU_POST 2
