@@ -172,6 +172,13 @@ int tb_rk_stage(tb_ctx* ctx, int stage, int t);   /* stage 1..4 of step t       
 int tb_step(tb_ctx* ctx, int t);                  /* four stages                 */
 int tb_steps(tb_ctx* ctx, int t0, int nsteps);    /* t0 .. t0+nsteps-1           */
 int tb_get_poisson_stats(tb_ctx* ctx, tb_poisson_stats* st);
+/* Mixed form, opt-in: the compact x-line operators (derparx, derparxx, the
+   x filter) of modes k >= 1, which hold only the disturbance, run in FP32
+   on FP64 data; mode 0 (the base flow and the 2D disturbance) stays FP64.
+   About 9% faster on the 1025 x 193 x 32 step, at the cost of ~1e-6
+   relative on the disturbance modes after two steps and 0.2-5e-6 after
+   eight: above the mixed form's 1e-6 target, hence off by default.  Default 0. */
+int tb_mixed_fp32_lines(tb_ctx* ctx, int on);
 /* Mixed form, P >= 16: the spanwise transforms of the disturbance products
    in the nonlinear terms run as DFT-matrix GEMMs on the tensor cores
    (split-BF16 operands, FP32 accumulation); 0 selects the FP32 FFT passes.

@@ -116,3 +116,28 @@ def test_mixed_rejects_tiny_coarse_grid(oracle_built):
     cfg, coefs, base = small_case(nx=33, precision=api.FORM_MIXED)   # coarsest level 9 points in x
     with pytest.raises(api.TbError):
         api.Context(cfg, coefs, base)
+
+
+def test_fp32_lines(mcase):
+    """x-line operators of modes k >= 1 in FP32 against FP64: the modes hold
+    only the disturbance (1e-3 of the base flow here), so the difference sits
+    at FP32 rounding of the disturbance."""
+    cfg, coefs, base, ora, api = mcase
+    g32 = api.Context(cfg, coefs, base)
+    g64 = api.Context(cfg, coefs, base)
+    g32.fp32_lines(True)
+    st = perturbed_state(cfg, base, np.random.default_rng(13))
+    for g in (g32, g64):
+        g.put_state(st)
+    t0 = cfg.stpp + 5
+    for t in (t0, t0 + 1):
+        g32.step(t)
+        g64.step(t)
+    a, b = g32.get_state(), g64.get_state()
+    for n in NAMES:
+        d = np.max(np.abs(a[n][1:] - b[n][1:]))        # modes k >= 1
+        s = np.max(np.abs(b[n][1:]))
+        assert d <= 1e-5 * s, n                        # FP32 differencing of the disturbance
+        assert np.array_equal(a[n][0], b[n][0]) or rel(a[n][0], b[n][0]) < 1e-8, n
+    g32.close()
+    g64.close()

@@ -120,6 +120,7 @@ def load():
     lib.tb_io_set_subrecord_limit.argtypes = [C.c_longlong]
     F = C.POINTER(C.c_float)
     lib.tb_nl_tensor_cores.argtypes = [P, C.c_int]
+    lib.tb_mixed_fp32_lines.argtypes = [P, C.c_int]
     lib.tb_dft_matrix.argtypes = [C.c_int, C.c_int, D]
     lib.tb_learn_init.argtypes = [P, C.c_ulonglong]
     lib.tb_learn_set_weights.argtypes = [P, F]
@@ -334,6 +335,9 @@ class Context:
 
     def write_pert(self, path):
         self._c(self.lib.tb_write_pert(self.h, os.fsencode(path)), "tb_write_pert")
+
+    def fp32_lines(self, on=True):
+        self._c(self.lib.tb_mixed_fp32_lines(self.h, 1 if on else 0), "tb_mixed_fp32_lines")
 
     def nl_tensor_cores(self, on=True):
         self._c(self.lib.tb_nl_tensor_cores(self.h, 1 if on else 0), "tb_nl_tensor_cores")

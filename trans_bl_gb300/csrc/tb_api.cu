@@ -138,7 +138,10 @@ int tb_destroy(tb_ctx* c) {
                     c->gibbs, c->delta_no, c->k2b2, c->tx1.a, c->tx1.g, c->tx1.ib, c->tx2.a, c->tx2.g, c->tx2.ib,
                     c->tfil.a, c->tfil.g, c->tfil.ib,
                     c->tx1.hf, c->tx1.hb, c->tx1.pf, c->tx1.pb, c->tx2.hf, c->tx2.hb, c->tx2.pf, c->tx2.pb,
-                    c->tfil.hf, c->tfil.hb, c->tfil.pf, c->tfil.pb, c->ty1.a, c->ty1.g, c->ty1.ib, c->tyfv.a, c->tyfv.g, c->tyfv.ib,
+                    c->tfil.hf, c->tfil.hb, c->tfil.pf, c->tfil.pb,
+                    c->tx1.af, c->tx1.gf, c->tx1.ibf, c->tx1.hff, c->tx1.hbf, c->tx1.pff, c->tx1.pbf,
+                    c->tx2.af, c->tx2.gf, c->tx2.ibf, c->tx2.hff, c->tx2.hbf, c->tx2.pff, c->tx2.pbf,
+                    c->tfil.af, c->tfil.gf, c->tfil.ibf, c->tfil.hff, c->tfil.hbf, c->tfil.pff, c->tfil.pbf, c->ty1.a, c->ty1.g, c->ty1.ib, c->tyfv.a, c->tyfv.g, c->tyfv.ib,
                     c->ty2.a, c->ty2.g, c->ty2.ib, c->ry1.w, c->ry1.off, c->ry1.cnt, c->ryfv.w, c->ryfv.off, c->ryfv.cnt,
                     c->ry2.w, c->ry2.off, c->ry2.cnt, c->px.lu, c->pfc, c->psc, c->pfct, c->pdef, c->pcarry,
                     c->pstate, c->perr, c->pqdy2, c->pcoef, c->wcoef};
@@ -271,6 +274,13 @@ int tb_steps(tb_ctx* c, int t0, int n) {
         int r = tb_step(c, t);
         if (r) return r;
     }
+    return TB_OK;
+}
+int tb_mixed_fp32_lines(tb_ctx* c, int on) {
+    if (!c) { tb_set_error("null context"); return TB_ERR_ARG; }
+    TB_CUDA(cudaStreamSynchronize(c->stream));
+    c->fp32_lines = on != 0;
+    tb_graph_reset(c);
     return TB_OK;
 }
 int tb_nl_tensor_cores(tb_ctx* c, int on) {

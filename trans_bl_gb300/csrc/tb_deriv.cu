@@ -14,102 +14,232 @@
 
 namespace {
 
-__device__ __forceinline__ cplx cmul(double s, cplx a) { return make_double2(s * a.x, s * a.y); }
-__device__ __forceinline__ cplx cadd(cplx a, cplx b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ cplx csub(cplx a, cplx b) { return make_double2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ cplx cfma(double s, cplx a, cplx b) { return make_double2(fma(s, a.x, b.x), fma(s, a.y, b.y)); }
+// Complex arithmetic in the working precision R (double, or float for the
+// mixed form's lines of modes k >= 1).
+template <class R> struct Cx;
+template <> struct Cx<double> { using V = double2; };
+template <> struct Cx<float> { using V = float2; };
+template <class V, class R> __device__ __forceinline__ V cmul(R s, V a) { return V{s * a.x, s * a.y}; }
+template <class V> __device__ __forceinline__ V cadd(V a, V b) { return V{a.x + b.x, a.y + b.y}; }
+template <class V> __device__ __forceinline__ V csub(V a, V b) { return V{a.x - b.x, a.y - b.y}; }
+template <class V, class R> __device__ __forceinline__ V cfma(R s, V a, V b) { return V{fma(s, a.x, b.x), fma(s, a.y, b.y)}; }
 
 struct XArgs {
     XJob job[8];
     int njobs, nx, ny, K;
+    int fp32_modes;   // lines of modes k >= 1 in FP32 (mixed form)
     double inv12dx, inv120dx, inv24dx, inv60dxx, inv360dxx, inv4dxx;
     double af, bf, cf, df;
     TriLHS t[3];
 };
 
-// A line staged in shared memory in lane chunks: row i at (i / S) * Sp + i % S
-// (Sp = S rounded up to odd, so the 16-byte accesses of 8 consecutive lanes
-// at the same chunk offset fall in distinct banks).
-struct SmemLine {
-    const cplx* F;
-    int S, Sp;
-    __device__ __forceinline__ cplx operator[](int i) const { return F[(i / S) * Sp + i % S]; }
+// The chunked Thomas tables of a TriLHS in precision R.
+template <class R> struct TriT;
+template <> struct TriT<double> {
+    const double *a, *g, *ib, *hf, *hb, *pf, *pb;
+    __device__ explicit TriT(const TriLHS& T) : a(T.a), g(T.g), ib(T.ib), hf(T.hf), hb(T.hb), pf(T.pf), pb(T.pb) {}
+};
+template <> struct TriT<float> {
+    const float *a, *g, *ib, *hf, *hb, *pf, *pb;
+    __device__ explicit TriT(const TriLHS& T) : a(T.af), g(T.gf), ib(T.ibf), hf(T.hff), hb(T.hbf), pf(T.pff), pb(T.pbf) {}
 };
 
-// RHS of one x-line point (rows 0-based); f is a pointer or a SmemLine.
-template <int OP, class Line>
-__device__ __forceinline__ cplx xrhs(const Line& f, int i, int n, const XArgs& A) {
+// A line staged in shared memory in lane chunks: row i at (i / S) * Sp + i % S
+// (Sp = S rounded up to odd, so the accesses of consecutive lanes at the
+// same chunk offset fall in distinct banks).
+template <class V>
+struct SmemLine {
+    const V* F;
+    int S, Sp;
+    __device__ __forceinline__ V operator[](int i) const { return F[(i / S) * Sp + i % S]; }
+};
+
+// RHS of one x-line point (rows 0-based); f is a SmemLine.
+template <int OP, class R, class Line>
+__device__ __forceinline__ typename Cx<R>::V xrhs(const Line& f, int i, int n, const XArgs& A) {
+    using V = typename Cx<R>::V;
     if (OP == XOP_D1) {
+        const R i12 = (R)A.inv12dx, i120 = (R)A.inv120dx, i24 = (R)A.inv24dx;
         if (i >= 2 && i < n - 2) {
-            cplx d2 = csub(f[i + 2], f[i - 2]), d1 = csub(f[i + 1], f[i - 1]);
-            return cmul(A.inv12dx, cfma(28.0, d1, d2));
+            V d2 = csub(f[i + 2], f[i - 2]), d1 = csub(f[i + 1], f[i - 1]);
+            return cmul(i12, cfma((R)28, d1, d2));
         }
         if (i == 0) {
-            cplx s = cmul(-25.0, f[0]); s = cfma(48.0, f[1], s); s = cfma(-36.0, f[2], s); s = cfma(16.0, f[3], s);
-            s = cfma(-3.0, f[4], s); return cmul(A.inv12dx, s);
+            V s = cmul((R)-25, f[0]); s = cfma((R)48, f[1], s); s = cfma((R)-36, f[2], s); s = cfma((R)16, f[3], s);
+            s = cfma((R)-3, f[4], s); return cmul(i12, s);
         }
         if (i == 1) {
-            cplx s = cmul(-406.0, f[0]); s = cfma(-300.0, f[1], s); s = cfma(760.0, f[2], s); s = cfma(-80.0, f[3], s);
-            s = cfma(30.0, f[4], s); s = cfma(-4.0, f[5], s); return cmul(A.inv120dx, s);
+            V s = cmul((R)-406, f[0]); s = cfma((R)-300, f[1], s); s = cfma((R)760, f[2], s); s = cfma((R)-80, f[3], s);
+            s = cfma((R)30, f[4], s); s = cfma((R)-4, f[5], s); return cmul(i120, s);
         }
         int m = n - 1;
         if (i == m - 1) {
-            cplx s = cmul(-406.0, f[m]); s = cfma(-300.0, f[m - 1], s); s = cfma(760.0, f[m - 2], s);
-            s = cfma(-80.0, f[m - 3], s); s = cfma(30.0, f[m - 4], s); s = cfma(-4.0, f[m - 5], s);
-            return cmul(-A.inv120dx, s);
+            V s = cmul((R)-406, f[m]); s = cfma((R)-300, f[m - 1], s); s = cfma((R)760, f[m - 2], s);
+            s = cfma((R)-80, f[m - 3], s); s = cfma((R)30, f[m - 4], s); s = cfma((R)-4, f[m - 5], s);
+            return cmul(-i120, s);
         }
-        cplx s = cmul(-74.0, f[m]); s = cfma(16.0, f[m - 1], s); s = cfma(72.0, f[m - 2], s); s = cfma(-16.0, f[m - 3], s);
-        s = cfma(2.0, f[m - 4], s); return cmul(-A.inv24dx, s);
+        V s = cmul((R)-74, f[m]); s = cfma((R)16, f[m - 1], s); s = cfma((R)72, f[m - 2], s); s = cfma((R)-16, f[m - 3], s);
+        s = cfma((R)2, f[m - 4], s); return cmul(-i24, s);
     } else if (OP == XOP_D2) {
+        const R i4 = (R)A.inv4dxx, i60 = (R)A.inv60dxx, i360 = (R)A.inv360dxx;
         if (i >= 2 && i < n - 2) {
-            cplx s2 = cadd(f[i + 2], f[i - 2]), s1 = cadd(f[i + 1], f[i - 1]);
-            cplx s = cmul(3.0, s2); s = cfma(48.0, s1, s); s = cfma(-102.0, f[i], s);
-            return cmul(A.inv4dxx, s);
+            V s2 = cadd(f[i + 2], f[i - 2]), s1 = cadd(f[i + 1], f[i - 1]);
+            V s = cmul((R)3, s2); s = cfma((R)48, s1, s); s = cfma((R)-102, f[i], s);
+            return cmul(i4, s);
         }
         int m = n - 1;
         int b = (i < 2) ? 0 : m;       // anchor
         int e = (i < 2) ? 1 : -1;      // direction
         if (i == 0 || i == m) {
-            cplx s = cmul(9775.0, f[b]); s = cfma(-20285.0, f[b + e], s); s = cfma(11170.0, f[b + 2 * e], s);
-            s = cfma(-550.0, f[b + 3 * e], s); s = cfma(-145.0, f[b + 4 * e], s); s = cfma(35.0, f[b + 5 * e], s);
-            return cmul(A.inv60dxx, s);
+            V s = cmul((R)9775, f[b]); s = cfma((R)-20285, f[b + e], s); s = cfma((R)11170, f[b + 2 * e], s);
+            s = cfma((R)-550, f[b + 3 * e], s); s = cfma((R)-145, f[b + 4 * e], s); s = cfma((R)35, f[b + 5 * e], s);
+            return cmul(i60, s);
         }
-        cplx s = cmul(4834.0, f[b]); s = cfma(-8424.0, f[b + e], s); s = cfma(1890.0, f[b + 2 * e], s);
-        s = cfma(2320.0, f[b + 3 * e], s); s = cfma(-810.0, f[b + 4 * e], s); s = cfma(216.0, f[b + 5 * e], s);
-        s = cfma(-26.0, f[b + 6 * e], s);
-        return cmul(A.inv360dxx, s);
+        V s = cmul((R)4834, f[b]); s = cfma((R)-8424, f[b + e], s); s = cfma((R)1890, f[b + 2 * e], s);
+        s = cfma((R)2320, f[b + 3 * e], s); s = cfma((R)-810, f[b + 4 * e], s); s = cfma((R)216, f[b + 5 * e], s);
+        s = cfma((R)-26, f[b + 6 * e], s);
+        return cmul(i360, s);
     } else {  // filter
         if (i >= 3 && i < n - 3) {
-            cplx s = cmul(A.af, f[i]);
-            s = cfma(A.bf, cadd(f[i + 1], f[i - 1]), s);
-            s = cfma(A.cf, cadd(f[i + 2], f[i - 2]), s);
-            s = cfma(A.df, cadd(f[i + 3], f[i - 3]), s);
+            V s = cmul((R)A.af, f[i]);
+            s = cfma((R)A.bf, cadd(f[i + 1], f[i - 1]), s);
+            s = cfma((R)A.cf, cadd(f[i + 2], f[i - 2]), s);
+            s = cfma((R)A.df, cadd(f[i + 3], f[i - 3]), s);
             return s;
         }
         int m = n - 1;
         int b = (i < 3) ? 0 : m;
         int e = (i < 3) ? 1 : -1;
         int r = (i < 3) ? i : m - i;
-        const double w0[3][5] = {{15, 4, -6, 4, -1}, {1, 12, 6, -4, 1}, {-1, 4, 10, 4, -1}};
-        cplx s = cmul(w0[r][0], f[b]);
+        const R w0[3][5] = {{15, 4, -6, 4, -1}, {1, 12, 6, -4, 1}, {-1, 4, 10, 4, -1}};
+        V s = cmul(w0[r][0], f[b]);
 #pragma unroll
         for (int q = 1; q < 5; q++) s = cfma(w0[r][q], f[b + q * e], s);
-        return cmul(0.0625, s);
+        return cmul((R)0.0625, s);
     }
 }
 
-// One warp per x-line (derparx/derparxx/filter_trid): the line is staged in
-// shared memory with coalesced loads; lane t owns rows [tS, tS + S) and runs
-// the Thomas sweeps over its chunk with zero carry-in, the carries of the
-// forward and backward sweeps cross the lanes by a Kogge-Stone scan of the
-// precomputed chunk responses (TriLHS pf/pb), and each row is fixed up with
-// its precomputed response hf/hb.  Shared memory per warp: 2 x 32 x Sp complex.
+template <class V> __device__ __forceinline__ V to_v(cplx c);
+template <> __device__ __forceinline__ double2 to_v<double2>(cplx c) { return c; }
+template <> __device__ __forceinline__ float2 to_v<float2>(cplx c) { return make_float2((float)c.x, (float)c.y); }
+__device__ __forceinline__ cplx to_c(double2 v) { return v; }
+__device__ __forceinline__ cplx to_c(float2 v) { return make_double2((double)v.x, (double)v.y); }
+
+// One x-line (derparx/derparxx/filter_trid) on one warp in precision R: the
+// line is staged in shared memory with coalesced loads; lane t owns rows
+// [tS, tS + S) and runs the Thomas sweeps over its chunk with zero carry-in,
+// the carries of the forward and backward sweeps cross the lanes by a
+// Kogge-Stone scan of the precomputed chunk responses (TriLHS pf/pb), and
+// each row is fixed up with its precomputed response hf/hb.  HBM stays FP64.
+template <int OP, class R>
+__device__ __forceinline__ void xline(const XArgs& A, const TriLHS& TL, const cplx* __restrict__ f, cplx* __restrict__ o,
+                                      void* wsm) {
+    using V = typename Cx<R>::V;
+    const TriT<R> T(TL);
+    const int lane = threadIdx.x & 31;
+    const int S = TL.S, Sp = S | 1, n = A.nx;
+    V* F = reinterpret_cast<V*>(wsm);
+    V* U = F + 32 * Sp;
+    for (int i = lane; i < n; i += 32) F[(i / S) * Sp + i % S] = to_v<V>(f[i]);
+    __syncwarp();
+    const SmemLine<V> L{F, S, Sp};
+    const int H = (OP == XOP_FILTER) ? 3 : 2;
+    const int r0 = lane * S, r1 = min(n, r0 + S);
+    V* Ul = U + lane * Sp;
+    // forward sweep over the chunk with zero carry-in
+    V u = V{0, 0};
+    int i = r0;
+    for (; i < r1 && i < H; i++) {
+        V r = xrhs<OP, R>(L, i, n, A);
+        R a = T.a[i], ib = T.ib[i];
+        u = V{(r.x - a * u.x) * ib, (r.y - a * u.y) * ib};
+        Ul[i - r0] = u;
+    }
+    if (i < r1 && i < n - H) {
+        V w[7];
+#pragma unroll
+        for (int q = 0; q < 2 * H; q++) w[q] = L[i - H + q];
+        int nc = (i + H) / S, no = (i + H) % S;   // chunk slot of row i + H
+        for (; i < r1 && i < n - H; i++) {
+            w[2 * H] = F[nc * Sp + no];
+            if (++no == S) { no = 0; nc++; }
+            V r;
+            if (OP == XOP_D1) {
+                V d2 = csub(w[4], w[0]), d1 = csub(w[3], w[1]);
+                r = cmul((R)A.inv12dx, cfma((R)28, d1, d2));
+            } else if (OP == XOP_D2) {
+                V q = cmul((R)3, cadd(w[4], w[0]));
+                q = cfma((R)48, cadd(w[3], w[1]), q);
+                q = cfma((R)-102, w[2], q);
+                r = cmul((R)A.inv4dxx, q);
+            } else {
+                V q = cmul((R)A.af, w[3]);
+                q = cfma((R)A.bf, cadd(w[4], w[2]), q);
+                q = cfma((R)A.cf, cadd(w[5], w[1]), q);
+                q = cfma((R)A.df, cadd(w[6], w[0]), q);
+                r = q;
+            }
+            R a = T.a[i], ib = T.ib[i];
+            u = V{(r.x - a * u.x) * ib, (r.y - a * u.y) * ib};
+            Ul[i - r0] = u;
+#pragma unroll
+            for (int q = 0; q < 2 * H; q++) w[q] = w[q + 1];
+        }
+    }
+    for (; i < r1; i++) {
+        V r = xrhs<OP, R>(L, i, n, A);
+        R a = T.a[i], ib = T.ib[i];
+        u = V{(r.x - a * u.x) * ib, (r.y - a * u.y) * ib};
+        Ul[i - r0] = u;
+    }
+    // forward carries: true chunk-end values by a scan, carry-in = previous lane's
+    V b = (r1 > r0) ? u : V{0, 0};
+#pragma unroll
+    for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
+        R ox = __shfl_up_sync(0xffffffffu, b.x, off), oy = __shfl_up_sync(0xffffffffu, b.y, off);
+        if (lane >= off) { R m = T.pf[d * 32 + lane]; b.x = fma(m, ox, b.x); b.y = fma(m, oy, b.y); }
+    }
+    V Uin;
+    Uin.x = __shfl_up_sync(0xffffffffu, b.x, 1); Uin.y = __shfl_up_sync(0xffffffffu, b.y, 1);
+    if (lane == 0) Uin = V{0, 0};
+    // forward fix-up fused with the backward sweep over the chunk (zero carry from the right)
+    V x = V{0, 0};
+    for (int q = r1 - 1; q >= r0; q--) {
+        R h = T.hf[q];
+        V uu = Ul[q - r0];
+        uu = V{fma(h, Uin.x, uu.x), fma(h, Uin.y, uu.y)};
+        if (q < r1 - 1) { R g = T.g[q + 1]; x = V{uu.x - g * x.x, uu.y - g * x.y}; }
+        else x = uu;
+        Ul[q - r0] = x;
+    }
+    // backward carries: true chunk-start values by a scan from the high lanes
+    b = (r1 > r0) ? x : V{0, 0};
+#pragma unroll
+    for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
+        R ox = __shfl_down_sync(0xffffffffu, b.x, off), oy = __shfl_down_sync(0xffffffffu, b.y, off);
+        if (lane + off < 32) { R m = T.pb[d * 32 + lane]; b.x = fma(m, ox, b.x); b.y = fma(m, oy, b.y); }
+    }
+    V Xin;
+    Xin.x = __shfl_down_sync(0xffffffffu, b.x, 1); Xin.y = __shfl_down_sync(0xffffffffu, b.y, 1);
+    if (lane == 31) Xin = V{0, 0};
+    for (int q = r0; q < r1; q++) {
+        R h = T.hb[q];
+        V xx = Ul[q - r0];
+        Ul[q - r0] = V{fma(h, Xin.x, xx.x), fma(h, Xin.y, xx.y)};
+    }
+    __syncwarp();
+    for (int q = lane; q < n; q += 32) o[q] = to_c(U[(q / S) * Sp + q % S]);
+}
+
+// One warp per x-line of the batched jobs; lines of modes k >= 1 run in FP32
+// when A.fp32_modes is set (the mixed form: they hold only the disturbance).
+// Shared memory per warp: 2 x 32 x Sp complex FP64 (the FP32 path uses half).
 template <int OP>
 __global__ void __launch_bounds__(64) k_xwarp(XArgs A) {
     extern __shared__ cplx xs[];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int wib = threadIdx.x >> 5;
     const TriLHS& T = A.t[OP];
-    const int S = T.S, Sp = S | 1, n = A.nx;
+    const int Sp = T.S | 1, n = A.nx;
     const long gw = (long)blockIdx.x * (blockDim.x >> 5) + wib;
     const int nlines = A.ny * A.K;
     const int jb = (int)(gw / nlines);
@@ -117,99 +247,11 @@ __global__ void __launch_bounds__(64) k_xwarp(XArgs A) {
     const XJob& J = A.job[jb];
     if (J.op != OP) return;
     const int line = (int)(gw - (long)jb * nlines);
-    cplx* F = xs + (size_t)wib * 64 * Sp;
-    cplx* U = F + 32 * Sp;
-    const cplx* __restrict__ f = J.src + (size_t)line * n;
-    cplx* __restrict__ o = J.dst + (size_t)line * n;
-    for (int i = lane; i < n; i += 32) F[(i / S) * Sp + i % S] = f[i];
-    __syncwarp();
-    const SmemLine L{F, S, Sp};
-    const int H = (OP == XOP_FILTER) ? 3 : 2;
-    const int r0 = lane * S, r1 = min(n, r0 + S);
-    cplx* Ul = U + lane * Sp;
-    // forward sweep over the chunk with zero carry-in
-    cplx u = make_double2(0.0, 0.0);
-    int i = r0;
-    for (; i < r1 && i < H; i++) {
-        cplx r = xrhs<OP>(L, i, n, A);
-        double a = T.a[i], ib = T.ib[i];
-        u = make_double2((r.x - a * u.x) * ib, (r.y - a * u.y) * ib);
-        Ul[i - r0] = u;
-    }
-    if (i < r1 && i < n - H) {
-        cplx w[7];
-#pragma unroll
-        for (int q = 0; q < 2 * H; q++) w[q] = L[i - H + q];
-        int nc = (i + H) / S, no = (i + H) % S;   // chunk slot of row i + H
-        for (; i < r1 && i < n - H; i++) {
-            w[2 * H] = F[nc * Sp + no];
-            if (++no == S) { no = 0; nc++; }
-            cplx r;
-            if (OP == XOP_D1) {
-                cplx d2 = csub(w[4], w[0]), d1 = csub(w[3], w[1]);
-                r = cmul(A.inv12dx, cfma(28.0, d1, d2));
-            } else if (OP == XOP_D2) {
-                cplx q = cmul(3.0, cadd(w[4], w[0]));
-                q = cfma(48.0, cadd(w[3], w[1]), q);
-                q = cfma(-102.0, w[2], q);
-                r = cmul(A.inv4dxx, q);
-            } else {
-                cplx q = cmul(A.af, w[3]);
-                q = cfma(A.bf, cadd(w[4], w[2]), q);
-                q = cfma(A.cf, cadd(w[5], w[1]), q);
-                q = cfma(A.df, cadd(w[6], w[0]), q);
-                r = q;
-            }
-            double a = T.a[i], ib = T.ib[i];
-            u = make_double2((r.x - a * u.x) * ib, (r.y - a * u.y) * ib);
-            Ul[i - r0] = u;
-#pragma unroll
-            for (int q = 0; q < 2 * H; q++) w[q] = w[q + 1];
-        }
-    }
-    for (; i < r1; i++) {
-        cplx r = xrhs<OP>(L, i, n, A);
-        double a = T.a[i], ib = T.ib[i];
-        u = make_double2((r.x - a * u.x) * ib, (r.y - a * u.y) * ib);
-        Ul[i - r0] = u;
-    }
-    // forward carries: true chunk-end values by a scan, carry-in = previous lane's
-    cplx b = (r1 > r0) ? u : make_double2(0.0, 0.0);
-#pragma unroll
-    for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
-        double ox = __shfl_up_sync(0xffffffffu, b.x, off), oy = __shfl_up_sync(0xffffffffu, b.y, off);
-        if (lane >= off) { double m = T.pf[d * 32 + lane]; b.x = fma(m, ox, b.x); b.y = fma(m, oy, b.y); }
-    }
-    cplx Uin;
-    Uin.x = __shfl_up_sync(0xffffffffu, b.x, 1); Uin.y = __shfl_up_sync(0xffffffffu, b.y, 1);
-    if (lane == 0) Uin = make_double2(0.0, 0.0);
-    // forward fix-up fused with the backward sweep over the chunk (zero carry from the right)
-    cplx x = make_double2(0.0, 0.0);
-    for (int q = r1 - 1; q >= r0; q--) {
-        double h = T.hf[q];
-        cplx uu = Ul[q - r0];
-        uu = make_double2(fma(h, Uin.x, uu.x), fma(h, Uin.y, uu.y));
-        if (q < r1 - 1) { double g = T.g[q + 1]; x = make_double2(uu.x - g * x.x, uu.y - g * x.y); }
-        else x = uu;
-        Ul[q - r0] = x;
-    }
-    // backward carries: true chunk-start values by a scan from the high lanes
-    b = (r1 > r0) ? x : make_double2(0.0, 0.0);
-#pragma unroll
-    for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
-        double ox = __shfl_down_sync(0xffffffffu, b.x, off), oy = __shfl_down_sync(0xffffffffu, b.y, off);
-        if (lane + off < 32) { double m = T.pb[d * 32 + lane]; b.x = fma(m, ox, b.x); b.y = fma(m, oy, b.y); }
-    }
-    cplx Xin;
-    Xin.x = __shfl_down_sync(0xffffffffu, b.x, 1); Xin.y = __shfl_down_sync(0xffffffffu, b.y, 1);
-    if (lane == 31) Xin = make_double2(0.0, 0.0);
-    for (int q = r0; q < r1; q++) {
-        double h = T.hb[q];
-        cplx xx = Ul[q - r0];
-        Ul[q - r0] = make_double2(fma(h, Xin.x, xx.x), fma(h, Xin.y, xx.y));
-    }
-    __syncwarp();
-    for (int q = lane; q < n; q += 32) o[q] = U[(q / S) * Sp + q % S];
+    void* wsm = xs + (size_t)wib * 64 * Sp;
+    const cplx* f = J.src + (size_t)line * n;
+    cplx* o = J.dst + (size_t)line * n;
+    if (A.fp32_modes && line >= A.ny) xline<OP, float>(A, T, f, o, wsm);   // line / ny = mode k >= 1
+    else xline<OP, double>(A, T, f, o, wsm);
 }
 
 struct YArgs {
@@ -279,6 +321,7 @@ int tb_launch_xlines(tb_ctx* c, const XJob* jobs, int njobs) {
         A.job[q] = jobs[q];
     }
     A.njobs = njobs; A.nx = c->g.nx; A.ny = c->g.ny; A.K = c->g.K;
+    A.fp32_modes = (c->cfg.precision == TB_FORM_MIXED && c->fp32_lines) ? 1 : 0;
     double dx = c->cfg.dx, dxx = dx * dx;
     A.inv12dx = 1.0 / (12.0 * dx); A.inv120dx = 1.0 / (120.0 * dx); A.inv24dx = 1.0 / (24.0 * dx);
     A.inv60dxx = 1.0 / (60.0 * dxx); A.inv360dxx = 1.0 / (360.0 * dxx); A.inv4dxx = 1.0 / (4.0 * dxx);

@@ -162,7 +162,12 @@ int upload_tri(TriLHS& t, const std::vector<double>& a, const std::vector<double
     if ((r = upload(&t.hf, hf))) return r;
     if ((r = upload(&t.hb, hb))) return r;
     if ((r = upload(&t.pf, pf))) return r;
-    return upload(&t.pb, pb);
+    if ((r = upload(&t.pb, pb))) return r;
+    auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+    if ((r = upload(&t.af, f32(a))) || (r = upload(&t.gf, f32(g))) || (r = upload(&t.ibf, f32(ib))) ||
+        (r = upload(&t.hff, f32(hf))) || (r = upload(&t.hbf, f32(hb))) || (r = upload(&t.pff, f32(pf))))
+        return r;
+    return upload(&t.pbf, f32(pb));
 }
 
 // lhs5 (loop_par.f:258-299) + ludecomp (penta_par.f:6-50), 1-based (n,5).

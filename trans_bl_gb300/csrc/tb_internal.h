@@ -48,6 +48,8 @@ struct TriLHS {
     double* pf = nullptr;   // (5, 32)
     double* pb = nullptr;   // (5, 32)
     int S = 0;
+    // FP32 copies of the chunked form (lines of the mixed form's modes k >= 1)
+    float *af = nullptr, *gf = nullptr, *ibf = nullptr, *hff = nullptr, *hbf = nullptr, *pff = nullptr, *pbf = nullptr;
 };
 // Row weights of the stretched-y compact RHS: row j (0-based) is
 // sum_m w[7*j+m] * f[j + off[j] + m], m < cnt[j].
@@ -142,6 +144,7 @@ struct tb_ctx {
     uint16_t* dft_tc = nullptr;            // BF16 DFT matrices (inverse hi, lo; forward hi, lo)
     int* tc_err = nullptr;                 // set when a bounded MMA wait ran out
     int sm_count = 0;
+    int fp32_lines = 0;                    // mixed form: line operators of modes k >= 1 in FP32 (opt-in)
 };
 
 // Kernel families timed by tb_profile (index into prof_ms / prof_n).
