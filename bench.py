@@ -353,8 +353,8 @@ def main():
             "breakdown_ms": dict({f: v[0] for f, v in fam.items()}, profiled_steps=prof_steps, profiled_total=prof_ms),
             "clocks": clk.summary()}
     if not args.no_e2e:
-        line["e2e"] = e2e_measure(ctx, cfg, t, max(1, min(args.steps, 3)), world, dist)
-        t += max(1, min(args.steps, 3))
+        line["e2e"] = e2e_measure(ctx, cfg, t, max(1, min(args.steps, 5)), world, dist)
+        t += max(1, min(args.steps, 5)) + 1
     st = ctx.get_state()
     ctx.close()
     if rank == 0 and world == 1 and form == "mixed" and not args.no_plain and state2 is not None:
@@ -457,6 +457,11 @@ def e2e_measure(ctx, cfg, t, steps, world, dist):
     D = C.POINTER(C.c_double)
     ptrs = [C.cast(host[n].data_ptr(), D) for n in NAMES]
     nbytes = sum(h.numel() * 8 for h in host.values())
+    # one untimed round trip (first use of the host buffers and of the step graph after host-launched steps)
+    api_check(ctx.lib.tb_put_state(ctx.h, *ptrs))
+    api_check(ctx.lib.tb_step(ctx.h, t))
+    api_check(ctx.lib.tb_get_state(ctx.h, *ptrs))
+    t += 1
     barrier(dist)
     t0 = time.perf_counter()
     for _ in range(steps):
