@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/tb_oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY: imported by the test suite, the smoke check and
-the CPU-baseline leg of bench.py as the checker; never by the library.
+the CPU-baseline leg of bench.py, to compare against; never by the library.
 Array conventions follow trans_bl_gb300.api (complex128, shape (K, ny, nx)).
 """
 import ctypes as C
