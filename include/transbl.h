@@ -181,7 +181,8 @@ int tb_get_poisson_stats(tb_ctx* ctx, tb_poisson_stats* st);
 int tb_mixed_fp32_lines(tb_ctx* ctx, int on);
 /* Mixed form, P >= 16: the spanwise transforms of the disturbance products
    in the nonlinear terms run as DFT-matrix GEMMs on the tensor cores
-   (split-BF16 operands, FP32 accumulation); 0 selects the FP32 FFT passes.
+   (operands split into three BF16 parts, products compensated to FP32
+   accuracy, FP32 accumulation); 0 selects the FP32 FFT passes.
    Default 1.                                                                */
 int tb_nl_tensor_cores(tb_ctx* ctx, int on);
 /* The DFT matrices of those GEMMs in double precision, P x P row-major:

@@ -1,7 +1,7 @@
 """Spanwise transforms of the mixed nonlinear terms on the tensor cores.
 
 The disturbance products go through two DFT-matrix GEMMs (tcgen05.mma,
-split-BF16 operands, FP32 accumulation); the mean terms stay in FP64.  The
+three-part split-BF16 operands, FP32 accumulation); the mean terms stay in FP64.  The
 result is checked against the FP64 oracle (nlterms_par.f) and against the
 FP32 FFT passes, on grids whose point count is not a multiple of the
 128-point tile, and through full mixed steps.
@@ -39,7 +39,7 @@ def test_nlterms_tensor_cores(oracle_built, grid):
     g.nl_tensor_cores(False)
     fft = g.nlterms()
     for a, f, b in zip(got, fft, want):
-        # split BF16 keeps ~16 bits of each operand against FP32's 24
+        # the DFT as a 64-term dot product against the FFT's butterflies
         dq, dt = np.max(np.abs(f - b)), np.max(np.abs(a - b))
         print("\nP=%d quadratic-term error: FP32 FFT %.2e, tensor cores %.2e" % (cfg.kphys, dq, dt))
         assert dt < max(1024.0 * dq, 1e-14)

@@ -295,8 +295,10 @@ __global__ void __launch_bounds__(128) k_nl_four(NlArgs A, const float* __restri
 
 // ---------------------------------------------------------------------------
 // The same two passes on the tensor cores: the spanwise transforms of the
-// disturbance as dense DFT-matrix GEMMs (tcgen05.mma, kind::f16), operands
-// split into BF16 high and low parts, a b ~ ah bh + ah bl + al bh,
+// disturbance as dense DFT-matrix GEMMs (tcgen05.mma, kind::f16), every FP32
+// operand split into three BF16 parts (x = x0 + x1 + x2 exactly, 8 bits each)
+// and the products compensated to FP32 accuracy,
+//   a b ~ a0 b0 + (a0 b1 + a1 b0) + (a0 b2 + a1 b1 + a2 b0),
 // accumulated in FP32 in tensor memory.  A tile is 128 points (one per
 // thread and tensor-memory lane); per point the P "slots" hold Re c0 (0: the
 // mean stays in FP64), Im c0 (the packed Nyquist term) and Re, Im of modes
@@ -308,11 +310,13 @@ __global__ void __launch_bounds__(128) k_nl_four(NlArgs A, const float* __restri
 // with R rows sits at (k / 8) * (R * 16) + r * 16 + (k % 8) * 2 bytes, so a
 // core matrix (8 rows x 8 k) is 128 contiguous bytes, core matrices
 // adjacent in rows are 128 bytes apart and those adjacent in k R * 16 apart.
+constexpr int TC_PARTS = 3;   // BF16 parts per FP32 operand
+
 template <int P>
 struct TcLayout {
     static constexpr int AB = 128 * P * 2, BB = P * P * 2;                 // bytes of one operand part
-    static constexpr int A_HI = 0, A_LO = AB, B_HI = 2 * AB, B_LO = 2 * AB + BB;
-    static constexpr int BAR = B_LO + BB;                                  // mbarrier, then the TMEM address
+    static constexpr int A0 = 0, B0 = TC_PARTS * AB;                       // part p at A0 + p AB, B0 + p BB
+    static constexpr int BAR = B0 + TC_PARTS * BB;                         // mbarrier, then the TMEM address
     static constexpr int BYTES = BAR + 16;
     static constexpr uint32_t NCOL = P < 32 ? 32 : P;                      // tensor-memory columns
     static constexpr uint32_t ID = tbtc::idesc_bf16_f32(128, P);
@@ -322,33 +326,42 @@ struct TcLayout {
     static constexpr int PER_SM = PER_SM0 < 8 ? PER_SM0 : 8;
 };
 
-__device__ __forceinline__ void split_bf16(float x, unsigned short& h, unsigned short& l) {
-    const __nv_bfloat16 hb = __float2bfloat16_rn(x);
-    const __nv_bfloat16 lb = __float2bfloat16_rn(x - __bfloat162float(hb));
-    h = __bfloat16_as_ushort(hb);
-    l = __bfloat16_as_ushort(lb);
+// x = x0 + x1 + x2 with BF16 parts (round to nearest at each step).
+__device__ __forceinline__ void split_bf16(float x, unsigned short* p) {
+#pragma unroll
+    for (int q = 0; q < TC_PARTS; q++) {
+        const __nv_bfloat16 b = __float2bfloat16_rn(x);
+        p[q] = __bfloat16_as_ushort(b);
+        x -= __bfloat162float(b);
+    }
 }
 
-// Row `row` of the A operand (P values) into its high and low parts.
+// Row `row` of the A operand (P values) into its BF16 parts.
 template <int P>
 __device__ __forceinline__ void stage_row(unsigned char* sm, int row, const float* v) {
     using Lt = TcLayout<P>;
 #pragma unroll
     for (int g = 0; g < P / 8; g++) {
-        unsigned short h[8], l[8];
+        unsigned short h[TC_PARTS][8];
 #pragma unroll
-        for (int e = 0; e < 8; e++) split_bf16(v[8 * g + e], h[e], l[e]);
-        uint4 H, L;
-        H.x = h[0] | ((uint32_t)h[1] << 16); H.y = h[2] | ((uint32_t)h[3] << 16);
-        H.z = h[4] | ((uint32_t)h[5] << 16); H.w = h[6] | ((uint32_t)h[7] << 16);
-        L.x = l[0] | ((uint32_t)l[1] << 16); L.y = l[2] | ((uint32_t)l[3] << 16);
-        L.z = l[4] | ((uint32_t)l[5] << 16); L.w = l[6] | ((uint32_t)l[7] << 16);
-        *reinterpret_cast<uint4*>(sm + Lt::A_HI + g * 2048 + row * 16) = H;
-        *reinterpret_cast<uint4*>(sm + Lt::A_LO + g * 2048 + row * 16) = L;
+        for (int e = 0; e < 8; e++) {
+            unsigned short p[TC_PARTS];
+            split_bf16(v[8 * g + e], p);
+#pragma unroll
+            for (int q = 0; q < TC_PARTS; q++) h[q][e] = p[q];
+        }
+#pragma unroll
+        for (int q = 0; q < TC_PARTS; q++) {
+            uint4 H;
+            H.x = h[q][0] | ((uint32_t)h[q][1] << 16); H.y = h[q][2] | ((uint32_t)h[q][3] << 16);
+            H.z = h[q][4] | ((uint32_t)h[q][5] << 16); H.w = h[q][6] | ((uint32_t)h[q][7] << 16);
+            *reinterpret_cast<uint4*>(sm + Lt::A0 + q * Lt::AB + g * 2048 + row * 16) = H;
+        }
     }
 }
 
-// One thread issues the tile's MMAs (3 per 16-wide k-step) and commits them.
+// One thread issues the tile's MMAs (the six part products of order <= 2
+// per 16-wide k-step) and commits them.
 template <int P>
 __device__ __forceinline__ void tile_mma(unsigned char* sm, uint32_t tmem, uint64_t* bar) {
     using Lt = TcLayout<P>;
@@ -356,25 +369,30 @@ __device__ __forceinline__ void tile_mma(unsigned char* sm, uint32_t tmem, uint6
 #pragma unroll
     for (int ks = 0; ks < P / 16; ks++) {
         const uint32_t ao = ks * 2 * 2048, bo = ks * 2 * P * 16;
-        const uint64_t ah = tbtc::sdesc(base + Lt::A_HI + ao, 2048, 128), al = tbtc::sdesc(base + Lt::A_LO + ao, 2048, 128);
-        const uint64_t bh = tbtc::sdesc(base + Lt::B_HI + bo, P * 16, 128), bl = tbtc::sdesc(base + Lt::B_LO + bo, P * 16, 128);
-        tbtc::mma_bf16(tmem, ah, bh, Lt::ID, ks > 0);
-        tbtc::mma_bf16(tmem, ah, bl, Lt::ID, 1);
-        tbtc::mma_bf16(tmem, al, bh, Lt::ID, 1);
+        uint64_t a[TC_PARTS], b[TC_PARTS];
+#pragma unroll
+        for (int q = 0; q < TC_PARTS; q++) {
+            a[q] = tbtc::sdesc(base + Lt::A0 + q * Lt::AB + ao, 2048, 128);
+            b[q] = tbtc::sdesc(base + Lt::B0 + q * Lt::BB + bo, P * 16, 128);
+        }
+        tbtc::mma_bf16(tmem, a[0], b[0], Lt::ID, ks > 0);
+        tbtc::mma_bf16(tmem, a[0], b[1], Lt::ID, 1);
+        tbtc::mma_bf16(tmem, a[1], b[0], Lt::ID, 1);
+        tbtc::mma_bf16(tmem, a[0], b[2], Lt::ID, 1);
+        tbtc::mma_bf16(tmem, a[1], b[1], Lt::ID, 1);
+        tbtc::mma_bf16(tmem, a[2], b[0], Lt::ID, 1);
     }
     tbtc::mma_commit(bar);
 }
 
-// Set-up shared by both passes: the constant B operand (high, low) into
+// Set-up shared by both passes: the constant B operand (its BF16 parts) into
 // shared memory, the mbarrier, and the tensor-memory columns.
 template <int P>
 __device__ __forceinline__ uint32_t tc_setup(unsigned char* sm, const uint16_t* mats) {
     using Lt = TcLayout<P>;
     const int t = threadIdx.x;
-    for (int i = t; i < P * P / 8; i += blockDim.x) {
-        reinterpret_cast<uint4*>(sm + Lt::B_HI)[i] = reinterpret_cast<const uint4*>(mats)[i];
-        reinterpret_cast<uint4*>(sm + Lt::B_LO)[i] = reinterpret_cast<const uint4*>(mats + P * P)[i];
-    }
+    for (int i = t; i < TC_PARTS * P * P / 8; i += blockDim.x)
+        reinterpret_cast<uint4*>(sm + Lt::B0)[i] = reinterpret_cast<const uint4*>(mats)[i];
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + Lt::BAR);
     uint32_t* slot = reinterpret_cast<uint32_t*>(sm + Lt::BAR + 8);
     if (t == 0) tbtc::mbar_init(bar, 1);
@@ -785,7 +803,7 @@ static void host_slots_from_phys(int P, const double* p, double* s) {
     }
 }
 
-// B operands of both passes, high and low BF16 parts, in the K-major core
+// B operands of both passes, their TC_PARTS BF16 parts, in the K-major core
 // layout of TcLayout: inverse (n = z, k = slot) then forward (n = slot, k = z).
 void tb_dft_matrices(int P, std::vector<uint16_t>& out) {
     std::vector<double> Tinv((size_t)P * P), Tfwd((size_t)P * P), e(P), v(P);
@@ -797,19 +815,21 @@ void tb_dft_matrices(int P, std::vector<uint16_t>& out) {
         host_slots_from_phys(P, e.data(), v.data());   // e as a physical unit vector at z = s
         for (int q = 0; q < P; q++) Tfwd[(size_t)q * P + s] = v[q];
     }
-    out.assign((size_t)4 * P * P, 0);
-    auto put = [&](int part, const std::vector<double>& T) {   // T[n][k]
+    out.assign((size_t)2 * TC_PARTS * P * P, 0);
+    auto put = [&](int first, const std::vector<double>& T) {   // T[n][k]
         for (int n = 0; n < P; n++)
             for (int k = 0; k < P; k++) {
-                const float x = (float)T[(size_t)n * P + k];
-                const uint16_t h = bf16_bits(x), l = bf16_bits(x - bf16_value(h));
+                float x = (float)T[(size_t)n * P + k];
                 const size_t o = (size_t)(k / 8) * (P * 8) + (size_t)n * 8 + (k % 8);
-                out[(size_t)part * P * P + o] = h;
-                out[(size_t)(part + 1) * P * P + o] = l;
+                for (int q = 0; q < TC_PARTS; q++) {
+                    const uint16_t h = bf16_bits(x);
+                    out[(size_t)(first + q) * P * P + o] = h;
+                    x -= bf16_value(h);
+                }
             }
     };
     put(0, Tinv);
-    put(2, Tfwd);
+    put(TC_PARTS, Tfwd);
 }
 
 // The two matrices in double precision, P x P row-major [n][k]: forward 0
@@ -908,7 +928,7 @@ int tb_launch_nlterms(tb_ctx* c, cplx* a, cplx* b, cplx* cc) {
         const unsigned g1 = (unsigned)std::min<size_t>(6 * tiles, cap), g2 = (unsigned)std::min<size_t>(3 * tiles, cap); \
         k_nl_phys_tc<PP><<<g1, 128, TcLayout<PP>::BYTES, c->stream>>>(A, c->nl_phys, c->dft_tc, c->tc_err);        \
         TB_CHECK_LAUNCH(c);                                                                                    \
-        k_nl_four_tc<PP><<<g2, 128, TcLayout<PP>::BYTES, c->stream>>>(A, c->nl_phys, c->dft_tc + 2 * PP * PP,      \
+        k_nl_four_tc<PP><<<g2, 128, TcLayout<PP>::BYTES, c->stream>>>(A, c->nl_phys, c->dft_tc + TC_PARTS * PP * PP, \
                                                                       c->tc_err);                              \
         break;                                                                                                 \
     }
