@@ -281,6 +281,7 @@ def main():
         cfg.step_graph = 0
     coefs, base = configs.setup_inputs(cfg)
     ctx = api.Context(cfg, coefs, base)
+    tune = ctx.autotune()   # launch shapes timed on this grid (scratch fields only)
     pts = cfg.nx * cfg.ny * cfg.kfour
     # start from a disturbed state past the one-period forcing ramp, so every
     # mode carries a disturbance and every solve does work
@@ -348,6 +349,7 @@ def main():
                        "step": "replayed CUDA graph" if (cfg.step_graph and form == "mixed") else "host-launched kernels",
                        "l2": "inputs larger than L2: working set ~5 GB vs 129 MB L2",
                        "start": "disturbed state (1e-3) past the forcing ramp",
+                       "launch_shapes": {k: tune[k] for k in ("xline_warps", "yline_threads", "nl_blocks_per_sm")},
                        "iterations_per_mode_last_solve": float(np.mean(stats["vcycles"][:cfg.kfour]))},
             "roofline": roof, "gpu_launches": launches,
             "breakdown_ms": dict({f: v[0] for f, v in fam.items()}, profiled_steps=prof_steps, profiled_total=prof_ms),

@@ -239,6 +239,19 @@ int tb_learn_forward(const float* w, const float* x, int n, int H, int W, float*
 int tb_learn_op_tables(tb_ctx* ctx, int k, float* tab);
 int tb_learn_op_apply(tb_ctx* ctx, int k, const float* e, float* out);
 
+/* ---- launch shapes ----------------------------------------------------
+   tb_autotune times the candidate launch shapes of the stage's batched
+   kernels on this context's grid and keeps the fastest: warps per block of
+   the x-line solves (1, 2), threads per block of the y-line solves (32, 64,
+   128) and, for the mixed form with P >= 16, resident blocks per SM of the
+   tensor-core passes (1, 2, 4, 8, capped by shared and tensor memory).  It
+   touches only scratch fields.  Times are per launch of the tuned batch.  */
+typedef struct tb_tune_result {
+    int   xline_warps, yline_threads, nl_blocks_per_sm;
+    float xline_ms, yline_ms, nl_ms;
+} tb_tune_result;
+int tb_autotune(tb_ctx* ctx, tb_tune_result* out);
+
 /* ---- ensembles: independent runs advanced together --------------------
    One recorded CUDA graph advances every member by one step: the members'
    stages run concurrently on the device and the host waits once per step.

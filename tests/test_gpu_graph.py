@@ -128,3 +128,29 @@ def test_ensemble_rejects_plain_member():
     with pytest.raises(api.TbError):
         api.Ensemble([g])
     g.close()
+
+
+def test_autotune_keeps_results():
+    """Tuned launch shapes move work between blocks, not between threads:
+    an autotuned context steps bit-identically to an untuned one."""
+    from trans_bl_gb300 import api
+    cfg, coefs, base = small_case(precision=api.FORM_MIXED, nx=65, ny=33, kfour=16, kphys=32, msh=3)
+    a = api.Context(cfg, coefs, base)
+    b = api.Context(cfg, coefs, base)
+    st = perturbed_state(cfg, base, np.random.default_rng(17))
+    a.put_state(st)
+    b.put_state(st)
+    r = a.autotune()
+    assert r["xline_warps"] in (1, 2) and r["yline_threads"] in (32, 64, 128)
+    assert r["nl_blocks_per_sm"] in (1, 2, 4, 8)
+    assert same_state_after(a, b, cfg.stpp + 1, 3)
+    a.close()
+    b.close()
+
+
+def same_state_after(a, b, t0, n):
+    for t in range(t0, t0 + n):
+        a.step(t)
+        b.step(t)
+    x, y = a.get_state(), b.get_state()
+    return all(np.array_equal(x[f], y[f]) for f in NAMES)

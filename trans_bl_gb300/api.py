@@ -56,6 +56,11 @@ class LearnStats(C.Structure):
                 ("kept", C.c_longlong), ("loss", C.c_double)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("xline_warps", C.c_int), ("yline_threads", C.c_int), ("nl_blocks_per_sm", C.c_int),
+                ("xline_ms", C.c_float), ("yline_ms", C.c_float), ("nl_ms", C.c_float)]
+
+
 class TbError(RuntimeError):
     pass
 
@@ -120,6 +125,7 @@ def load():
     lib.tb_io_set_subrecord_limit.argtypes = [C.c_longlong]
     F = C.POINTER(C.c_float)
     lib.tb_nl_tensor_cores.argtypes = [P, C.c_int]
+    lib.tb_autotune.argtypes = [P, C.POINTER(TuneResult)]
     lib.tb_mixed_fp32_lines.argtypes = [P, C.c_int]
     lib.tb_dft_matrix.argtypes = [C.c_int, C.c_int, D]
     lib.tb_learn_init.argtypes = [P, C.c_ulonglong]
@@ -335,6 +341,12 @@ class Context:
 
     def write_pert(self, path):
         self._c(self.lib.tb_write_pert(self.h, os.fsencode(path)), "tb_write_pert")
+
+    def autotune(self):
+        """Time the candidate launch shapes on this grid and keep the fastest (tb_autotune)."""
+        r = TuneResult()
+        self._c(self.lib.tb_autotune(self.h, C.byref(r)), "tb_autotune")
+        return {n: getattr(r, n) for n, _ in TuneResult._fields_}
 
     def fp32_lines(self, on=True):
         self._c(self.lib.tb_mixed_fp32_lines(self.h, 1 if on else 0), "tb_mixed_fp32_lines")

@@ -332,7 +332,7 @@ int tb_launch_xlines(tb_ctx* c, const XJob* jobs, int njobs) {
     size_t lines = (size_t)njobs * c->g.ny * c->g.K;   // one warp each
     bool has[3] = {false, false, false};
     for (int q = 0; q < njobs; q++) has[jobs[q].op] = true;
-    const int WPB = 2;
+    const int WPB = c->tune_xw == 1 ? 1 : 2;   // warps per block (tb_autotune), at most 2 (launch bounds)
     int Sp = c->tx1.S | 1;
     size_t smem = (size_t)WPB * 64 * Sp * sizeof(cplx);
     unsigned nb = tb_blocks(lines, WPB);
@@ -372,11 +372,12 @@ int tb_launch_ylines(tb_ctx* c, const YJob* jobs, int njobs) {
     size_t total = (size_t)njobs * c->g.nx * c->g.K;
     bool has[3] = {false, false, false};
     for (int q = 0; q < njobs; q++) has[jobs[q].op] = true;
-    unsigned nb = tb_blocks(total, 128);
+    const int yt = (c->tune_yt == 32 || c->tune_yt == 64) ? c->tune_yt : 128;   // threads per block (tb_autotune)
+    unsigned nb = tb_blocks(total, yt);
     cudaEvent_t ps = nullptr;
     if (tb_prof_begin(c, PROF_YLINES, &ps)) return TB_ERR_CUDA;
-    if (has[0]) { k_ylines<YOP_D1><<<nb, 128, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
-    if (has[1]) { k_ylines<YOP_D1FV><<<nb, 128, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
-    if (has[2]) { k_ylines<YOP_D2><<<nb, 128, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
+    if (has[0]) { k_ylines<YOP_D1><<<nb, yt, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
+    if (has[1]) { k_ylines<YOP_D1FV><<<nb, yt, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
+    if (has[2]) { k_ylines<YOP_D2><<<nb, yt, 0, c->stream>>>(A); TB_CHECK_LAUNCH(c); }
     return tb_prof_end(c, PROF_YLINES, ps);
 }

@@ -145,6 +145,10 @@ struct tb_ctx {
     int* tc_err = nullptr;                 // set when a bounded MMA wait ran out
     int sm_count = 0;
     int fp32_lines = 0;                    // mixed form: line operators of modes k >= 1 in FP32 (opt-in)
+    // launch shapes chosen by tb_autotune (0: the built-in defaults)
+    int tune_xw = 0;                       // warps per block of the x-line kernel (1 or 2)
+    int tune_yt = 0;                       // threads per block of the y-line kernel (32, 64 or 128)
+    int tune_nl = 0;                       // resident blocks per SM of the tensor-core passes
 };
 
 // Kernel families timed by tb_profile (index into prof_ms / prof_n).

@@ -924,7 +924,8 @@ int tb_launch_nlterms(tb_ctx* c, cplx* a, cplx* b, cplx* cc) {
         switch (P) {
 #define TB_TC_CASE(PP)                                                                                        \
     case PP: {                                                                                                 \
-        const size_t cap = (size_t)TcLayout<PP>::PER_SM * sms;                                                 \
+        const int per = (c->tune_nl >= 1 && c->tune_nl <= TcLayout<PP>::PER_SM) ? c->tune_nl : TcLayout<PP>::PER_SM; \
+        const size_t cap = (size_t)per * sms;                                                                  \
         const unsigned g1 = (unsigned)std::min<size_t>(6 * tiles, cap), g2 = (unsigned)std::min<size_t>(3 * tiles, cap); \
         k_nl_phys_tc<PP><<<g1, 128, TcLayout<PP>::BYTES, c->stream>>>(A, c->nl_phys, c->dft_tc, c->tc_err);        \
         TB_CHECK_LAUNCH(c);                                                                                    \
