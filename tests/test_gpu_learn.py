@@ -142,6 +142,40 @@ def test_learned_solve(trained):
     learned.close()
 
 
+def test_learned_other_frequency(trained):
+    """Weights trained at F = 1e-4 applied to a run at F = 1.2e-4: the
+    fields still agree with the run without the network (both iterate to the
+    tolerance); the share of kept corrections and the corrections per step
+    are reported."""
+    from trans_bl_gb300 import api, configs
+    cfg0, coefs, base, state, t, w, _, _ = trained
+    cfg = configs.blasius_ts_config(257, 97, 8, 16, 4, precision=api.FORM_MIXED, amp2d=1e-4, amp3d=1e-5,
+                                    n_lambda=6.0, strip=(1.0, 1.6), F=1.2e-4)
+    cfg.stpp = configs.stable_steps_per_period(cfg)
+    coefs, base = configs.setup_inputs(cfg)
+    st = perturbed_state(cfg, base, np.random.default_rng(32))
+    plain = api.Context(cfg, coefs, base)
+    learned = api.Context(cfg, coefs, base)
+    learned.learn_set_weights(w)
+    learned.learn_enable(True)
+    t1 = cfg.stpp + 1
+    for c in (plain, learned):
+        c.put_state(st)
+        corrections(c, t1, 2)
+    n = 16
+    c_plain = corrections(plain, t1 + 2, n)
+    c_learned = corrections(learned, t1 + 2, n)
+    s = learned.learn_stats()
+    a, b = learned.get_state(), plain.get_state()
+    for f in NAMES:
+        assert rel(a[f], b[f]) < 1e-6, f
+    print("\nF = 1.2e-4 with weights from F = 1e-4: corrections over %d steps %d -> %d; kept %d of %d"
+          % (n, c_plain, c_learned, s["kept"], s["tried"]))
+    assert c_learned <= 1.1 * c_plain
+    plain.close()
+    learned.close()
+
+
 def test_learned_graph_matches_host_launched(trained):
     from trans_bl_gb300 import api
     cfg, coefs, base, state, t, w, _, _ = trained
