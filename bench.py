@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     p.add_argument("--no-ensemble", action="store_true", help="skip the 12-run ensemble measurement")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the default launch shapes (profiler captures: the tuner's trial launches come first)")
     p.add_argument("--no-graph", action="store_true",
                    help="launch every kernel from the host (same kernels; for profilers that cannot enter "
                         "graphs with conditional nodes)")
@@ -281,7 +283,8 @@ def main():
         cfg.step_graph = 0
     coefs, base = configs.setup_inputs(cfg)
     ctx = api.Context(cfg, coefs, base)
-    tune = ctx.autotune()   # launch shapes timed on this grid (scratch fields only)
+    # launch shapes timed on this grid (scratch fields only)
+    tune = ({"xline_warps": 0, "yline_threads": 0, "nl_blocks_per_sm": 0} if args.no_autotune else ctx.autotune())
     pts = cfg.nx * cfg.ny * cfg.kfour
     # start from a disturbed state past the one-period forcing ramp, so every
     # mode carries a disturbance and every solve does work
