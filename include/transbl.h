@@ -185,6 +185,12 @@ int tb_mixed_fp32_lines(tb_ctx* ctx, int on);
    accuracy, FP32 accumulation); 0 selects the FP32 FFT passes.
    Default 1.                                                                */
 int tb_nl_tensor_cores(tb_ctx* ctx, int on);
+/* Tests of the error path only: with on = 1 the tensor-core passes leave
+   their MMAs unissued and wait at most a few thousand polls, so the bounded
+   wait runs out; the kernels free their tensor memory and return, and the
+   next synchronising call reports TB_ERR_TIMEOUT.  No MMA is in flight and
+   nothing faults; the context stays usable.                                */
+int tb_tc_timeout_test(tb_ctx* ctx, int on);
 /* The DFT matrices of those GEMMs in double precision, P x P row-major:
    forward 0: physical z from slot s (slots: Re c0 (unused), Im c0 as the
    Nyquist term, Re and Im of modes 1 .. P/2-1); forward 1: slot from z.     */

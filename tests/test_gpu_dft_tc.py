@@ -58,3 +58,20 @@ def test_steps_tensor_cores(oracle_built):
         assert rel(a[n], b[n]) < 1e-6, n
     g.close()
     o.close()
+
+
+def test_bounded_wait_times_out(oracle_built):
+    """The tensor-core passes' wait for their MMAs is bounded: with the MMAs
+    left unissued (a test switch) the wait runs out after a few thousand
+    polls, the kernels free their tensor memory and return, the call reports
+    TB_ERR_TIMEOUT, and the context computes correctly afterwards."""
+    from trans_bl_gb300 import api
+    cfg, g, o = pair(oracle_built, GRIDS[0], 5)
+    api.check(g.lib.tb_tc_timeout_test(g.h, 1), "tb_tc_timeout_test")
+    with pytest.raises(api.TbError, match="bounded wait"):
+        g.nlterms()
+    api.check(g.lib.tb_tc_timeout_test(g.h, 0), "tb_tc_timeout_test")
+    for a, b in zip(g.nlterms(), o.nlterms()):
+        assert rel(a, b) < 1e-8
+    g.close()
+    o.close()

@@ -125,6 +125,7 @@ def load():
     lib.tb_io_set_subrecord_limit.argtypes = [C.c_longlong]
     F = C.POINTER(C.c_float)
     lib.tb_nl_tensor_cores.argtypes = [P, C.c_int]
+    lib.tb_tc_timeout_test.argtypes = [P, C.c_int]
     lib.tb_autotune.argtypes = [P, C.POINTER(TuneResult)]
     lib.tb_mixed_fp32_lines.argtypes = [P, C.c_int]
     lib.tb_dft_matrix.argtypes = [C.c_int, C.c_int, D]

@@ -55,7 +55,15 @@ int copy_field(tb_ctx* c, void* dst, const void* src, size_t bytes, bool to_devi
     return TB_OK;
 }
 int up(tb_ctx* c, cplx* d, const double* h, size_t n) { return copy_field(c, d, h, n * sizeof(cplx), true); }
-int down(tb_ctx* c, double* h, const cplx* d, size_t n) { return copy_field(c, h, d, n * sizeof(cplx), false); }
+// Device -> host, complete on return (the mirrors hand the buffer back at once).
+int down(tb_ctx* c, double* h, const cplx* d, size_t n) {
+    int r = copy_field(c, h, d, n * sizeof(cplx), false);
+    if (r) return r;
+    TB_CUDA(cudaStreamSynchronize(c->stream));
+    return TB_OK;
+}
+// Device -> host, queued only: the caller waits once after its last copy.
+int down_async(tb_ctx* c, double* h, const cplx* d, size_t n) { return copy_field(c, h, d, n * sizeof(cplx), false); }
 int finish(tb_ctx* c) {
     TB_CUDA(cudaGetLastError());
     TB_CUDA(cudaStreamSynchronize(c->stream));
@@ -220,8 +228,8 @@ int tb_get_state(tb_ctx* c, double* ux, double* uy, double* uz, double* wx, doub
     if (!c || !ux || !uy || !uz || !wx || !wy || !wz) { tb_set_error("null argument"); return TB_ERR_ARG; }
     size_t n3 = tb_n3(c);
     int r;
-    if ((r = down(c, ux, c->ux, n3)) || (r = down(c, uy, c->uy, n3)) || (r = down(c, uz, c->uz, n3)) ||
-        (r = down(c, wx, c->wx, n3)) || (r = down(c, wy, c->wy, n3)) || (r = down(c, wz, c->wz, n3)))
+    if ((r = down_async(c, ux, c->ux, n3)) || (r = down_async(c, uy, c->uy, n3)) || (r = down_async(c, uz, c->uz, n3)) ||
+        (r = down_async(c, wx, c->wx, n3)) || (r = down_async(c, wy, c->wy, n3)) || (r = down_async(c, wz, c->wz, n3)))
         return r;
     return finish(c);
 }
@@ -232,7 +240,7 @@ int tb_put_wall(tb_ctx* c, const double* d) {
 }
 int tb_get_wall(tb_ctx* c, double* d) {
     if (!c || !d) { tb_set_error("null argument"); return TB_ERR_ARG; }
-    int r = down(c, d, c->d2uydx2, (size_t)c->g.nx * c->g.K);
+    int r = down_async(c, d, c->d2uydx2, (size_t)c->g.nx * c->g.K);
     return r ? r : finish(c);
 }
 
@@ -283,6 +291,13 @@ int tb_mixed_fp32_lines(tb_ctx* c, int on) {
     tb_graph_reset(c);
     return TB_OK;
 }
+int tb_tc_timeout_test(tb_ctx* c, int on) {
+    if (!c) { tb_set_error("null context"); return TB_ERR_ARG; }
+    TB_CUDA(cudaStreamSynchronize(c->stream));
+    c->tc_timeout_test = on != 0;
+    tb_graph_reset(c);
+    return TB_OK;
+}
 int tb_nl_tensor_cores(tb_ctx* c, int on) {
     if (!c) { tb_set_error("null context"); return TB_ERR_ARG; }
     TB_CUDA(cudaStreamSynchronize(c->stream));
@@ -327,7 +342,7 @@ int tb_nlterms(tb_ctx* c, double* a, double* b, double* cc) {
     if ((r = tb_launch_nlterms(c, c->tmp[0], c->tmp[1], c->tmp[2]))) return r;
     size_t n3 = tb_n3(c);
     if ((r = down(c, a, c->tmp[0], n3)) || (r = down(c, b, c->tmp[1], n3)) || (r = down(c, cc, c->tmp[2], n3))) return r;
-    return TB_OK;
+    return tb_tc_check(c);
 }
 int tb_drv(tb_ctx* c, double* x, double* y, double* z) {
     if (!ready(c)) return TB_ERR_STATE;

@@ -143,6 +143,7 @@ struct tb_ctx {
     int nl_tensor = 1;                     // 0: the FP32 FFT passes instead
     uint16_t* dft_tc = nullptr;            // BF16 DFT matrices (inverse hi, lo; forward hi, lo)
     int* tc_err = nullptr;                 // set when a bounded MMA wait ran out
+    int tc_timeout_test = 0;               // tests only: the passes skip their MMAs so the bounded wait runs out
     int sm_count = 0;
     int fp32_lines = 0;                    // mixed form: line operators of modes k >= 1 in FP32 (opt-in)
     // launch shapes chosen by tb_autotune (0: the built-in defaults)

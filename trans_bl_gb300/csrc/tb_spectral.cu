@@ -408,17 +408,24 @@ __device__ __forceinline__ uint32_t tc_setup(unsigned char* sm, const uint16_t* 
 
 // Issue, wait (bounded) and read: returns false (for the whole block) when
 // the wait ran out, after which the caller stops issuing.
+// TcCtl: the wait limit in polls and, for tests of the time-out path only,
+// a switch that leaves the MMAs unissued so that the wait runs out.
+struct TcCtl {
+    uint32_t limit;
+    int skip_mma;
+};
+
 template <int P>
-__device__ __forceinline__ bool tc_run(unsigned char* sm, uint32_t tmem, uint32_t& phase) {
+__device__ __forceinline__ bool tc_run(unsigned char* sm, uint32_t tmem, uint32_t& phase, const TcCtl& ctl) {
     using Lt = TcLayout<P>;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + Lt::BAR);
     tbtc::fence_async_smem();
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && !ctl.skip_mma) {
         tbtc::fence_after_sync();
         tile_mma<P>(sm, tmem, bar);
     }
-    const bool ok = tbtc::mbar_wait(bar, phase);
+    const bool ok = tbtc::mbar_wait(bar, phase, ctl.limit);
     tbtc::fence_after_sync();
     const bool all = !__syncthreads_or(!ok);
     if (all) phase ^= 1u;   // on a time-out `phase` stays that of the tile in flight
@@ -426,10 +433,11 @@ __device__ __forceinline__ bool tc_run(unsigned char* sm, uint32_t tmem, uint32_
 }
 
 template <int P>
-__device__ __forceinline__ void tc_teardown(unsigned char* sm, uint32_t tmem, bool ok, uint32_t phase, int* err) {
+__device__ __forceinline__ void tc_teardown(unsigned char* sm, uint32_t tmem, bool ok, uint32_t phase, int* err,
+                                            const TcCtl& ctl) {
     using Lt = TcLayout<P>;
     if (!ok) {   // let the MMAs of the abandoned tile finish (bounded) before freeing their columns
-        (void)tbtc::mbar_wait(reinterpret_cast<uint64_t*>(sm + Lt::BAR), phase);
+        (void)tbtc::mbar_wait(reinterpret_cast<uint64_t*>(sm + Lt::BAR), phase, ctl.limit);
         if (threadIdx.x == 0) atomicExch(err, 1);
     }
     tbtc::fence_before_sync();
@@ -445,7 +453,7 @@ __device__ __forceinline__ const cplx* nl_field(const NlArgs& A, int f) {
 // Pass 1 on the tensor cores: tile = (field f, 128 points) -> ph[(f P + z) n2 + q].
 template <int P>
 __global__ void __launch_bounds__(128) k_nl_phys_tc(NlArgs A, float* __restrict__ ph, const uint16_t* __restrict__ mats,
-                                                    int* err) {
+                                                    int* err, TcCtl ctl) {
     constexpr int N = P / 2;
     extern __shared__ __align__(1024) unsigned char sm[];
     const uint32_t tmem = tc_setup<P>(sm, mats);
@@ -469,7 +477,7 @@ __global__ void __launch_bounds__(128) k_nl_phys_tc(NlArgs A, float* __restrict_
             v[2 * k + 1] = (float)c.y;
         }
         stage_row<P>(sm, t, v);
-        if (!(ok = tc_run<P>(sm, tmem, phase))) break;
+        if (!(ok = tc_run<P>(sm, tmem, phase, ctl))) break;
 #pragma unroll
         for (int c0 = 0; c0 < P; c0 += 16) {
             float w[16];
@@ -482,14 +490,14 @@ __global__ void __launch_bounds__(128) k_nl_phys_tc(NlArgs A, float* __restrict_
         tbtc::fence_before_sync();
         __syncthreads();
     }
-    tc_teardown<P>(sm, tmem, ok, phase, err);
+    tc_teardown<P>(sm, tmem, ok, phase, err, ctl);
 }
 
 // Pass 2 on the tensor cores: tile = (output o, 128 points); the quadratic
 // disturbance term's slots plus the FP64 mean terms, as k_nl_four.
 template <int P>
 __global__ void __launch_bounds__(128) k_nl_four_tc(NlArgs A, const float* __restrict__ ph,
-                                                    const uint16_t* __restrict__ mats, int* err) {
+                                                    const uint16_t* __restrict__ mats, int* err, TcCtl ctl) {
     constexpr int N = P / 2;
     extern __shared__ __align__(1024) unsigned char sm[];
     const uint32_t tmem = tc_setup<P>(sm, mats);
@@ -516,7 +524,7 @@ __global__ void __launch_bounds__(128) k_nl_four_tc(NlArgs A, const float* __res
             }
         }
         stage_row<P>(sm, t, v);
-        if (!(ok = tc_run<P>(sm, tmem, phase))) break;
+        if (!(ok = tc_run<P>(sm, tmem, phase, ctl))) break;
 #pragma unroll
         for (int c0 = 0; c0 < P; c0 += 16) tbtc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v + c0);
         if (q < n2) {
@@ -537,7 +545,7 @@ __global__ void __launch_bounds__(128) k_nl_four_tc(NlArgs A, const float* __res
         tbtc::fence_before_sync();
         __syncthreads();
     }
-    tc_teardown<P>(sm, tmem, ok, phase, err);
+    tc_teardown<P>(sm, tmem, ok, phase, err, ctl);
 }
 
 // Smagorinsky eddy viscosity and force nu_t lap(u) (les_par.f:6-211).
@@ -921,16 +929,18 @@ int tb_launch_nlterms(tb_ctx* c, cplx* a, cplx* b, cplx* cc) {
         if (!c->capturing && (r = tb_spectral_prepare(c))) return r;
         const int P = c->g.P, sms = c->sm_count > 0 ? c->sm_count : 148;
         const size_t tiles = (A.n2 + 127) / 128;
+        // a time-out test shortens the wait to a few thousand polls and leaves the MMAs unissued
+        const TcCtl ctl{c->tc_timeout_test ? 4096u : (1u << 22), c->tc_timeout_test};
         switch (P) {
 #define TB_TC_CASE(PP)                                                                                        \
     case PP: {                                                                                                 \
         const int per = (c->tune_nl >= 1 && c->tune_nl <= TcLayout<PP>::PER_SM) ? c->tune_nl : TcLayout<PP>::PER_SM; \
         const size_t cap = (size_t)per * sms;                                                                  \
         const unsigned g1 = (unsigned)std::min<size_t>(6 * tiles, cap), g2 = (unsigned)std::min<size_t>(3 * tiles, cap); \
-        k_nl_phys_tc<PP><<<g1, 128, TcLayout<PP>::BYTES, c->stream>>>(A, c->nl_phys, c->dft_tc, c->tc_err);        \
+        k_nl_phys_tc<PP><<<g1, 128, TcLayout<PP>::BYTES, c->stream>>>(A, c->nl_phys, c->dft_tc, c->tc_err, ctl);   \
         TB_CHECK_LAUNCH(c);                                                                                    \
         k_nl_four_tc<PP><<<g2, 128, TcLayout<PP>::BYTES, c->stream>>>(A, c->nl_phys, c->dft_tc + TC_PARTS * PP * PP, \
-                                                                      c->tc_err);                              \
+                                                                      c->tc_err, ctl);                         \
         break;                                                                                                 \
     }
             TB_TC_CASE(16)
