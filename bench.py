@@ -17,7 +17,7 @@ plain_fp64   : (with --form mixed) the plain FP64 form timed in the same run
                from the same state, its mean V-cycles, the step-level byte
                model, and the mixed-vs-plain field error after two steps.
 cpu_baseline : the oracle (C++ restatement of the reference CPU path) timed
-               on one RK stage of the same state on all host threads.
+               on one RK4 step of the same state on all host threads.
 With --impl reference the whole line times that restatement instead.
 """
 import argparse
@@ -166,15 +166,16 @@ def start_state(cfg, base):
     return configs.disturbed_state(cfg, base, np.random.default_rng(5))
 
 
-def cpu_stage_seconds(cfg, coefs, base, state, threads, t):
-    """One RK stage of the oracle on the given state, on `threads` host threads (s)."""
+def cpu_step_seconds(cfg, coefs, base, state, threads, t):
+    """One RK4 step (four stages, the filter in the fourth) of the oracle on
+    the given state, on `threads` host threads (s)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as ora
     used = ora.set_threads(threads)
     o = ora.Oracle(cfg, coefs, base)
     o.put_state(state)
     t0 = time.perf_counter()
-    o.rk_stage(1, t)
+    o.step(t)
     el = time.perf_counter() - t0
     o.close()
     return el, used
@@ -194,15 +195,15 @@ def run_reference(args, rank, world):
     steps = max(1, min(args.steps, 2))
     used = threads
     for _ in range(warm):
-        _, used = cpu_stage_seconds(cfg, coefs, base, st, threads, cfg.stpp + 1)
+        _, used = cpu_step_seconds(cfg, coefs, base, st, threads, cfg.stpp + 1)
     times = []
     for _ in range(steps):
-        el, used = cpu_stage_seconds(cfg, coefs, base, st, threads, cfg.stpp + 1)
+        el, used = cpu_step_seconds(cfg, coefs, base, st, threads, cfg.stpp + 1)
         times.append(el)
-    ms_per_step = 4.0 * 1e3 * float(np.median(times))
+    ms_per_step = 1e3 * float(np.median(times))
     value = pts / (ms_per_step * 1e-3) / 1e6
-    sample = ("one RK stage (of four) of the nx=1025 ny=193 K=32 step from the benchmark's start state, "
-              "median of %d samples; per-step time = 4 x stage" % steps)
+    sample = ("one RK4 step (four stages) of the nx=1025 ny=193 K=32 workload from the benchmark's start state, "
+              "median of %d samples after %d warm-up" % (steps, warm))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpt-steps/s", "n_gpus": world,
             "steps": steps, "warmup": warm, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -370,11 +371,11 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         pcfg = workload("plain")
         threads = os.cpu_count() or 1
-        cpu_s, used = cpu_stage_seconds(pcfg, coefs, base, st, threads, t)
-        cpu_val = pts / (4.0 * cpu_s) / 1e6
+        cpu_s, used = cpu_step_seconds(pcfg, coefs, base, st, threads, t)
+        cpu_val = pts / cpu_s / 1e6
         line["cpu_baseline"] = {"value": cpu_val, "unit": "Mpt-steps/s", "cores": used, "kind": "port",
-                                "sample": "one RK stage of the same nx=1025 ny=193 K=32 state on %d host threads "
-                                          "(%.2f s); per-step rate = stage rate / 4" % (used, cpu_s)}
+                                "sample": "one RK4 step (four stages) of the same nx=1025 ny=193 K=32 state on %d "
+                                          "host threads (%.2f s)" % (used, cpu_s)}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
