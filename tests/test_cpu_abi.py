@@ -39,3 +39,32 @@ def test_bad_configs_are_rejected(lib_built):
 
 def test_coef_count(lib_built):
     assert lib_built.tb_coef_count(4) == 100 + 24 * 4
+
+
+def header_prototypes():
+    src = open(os.path.join(ROOT, "include", "transbl.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return {m.group(1): m.group(2) for m in re.finditer(r"\b(tb_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src)}
+
+
+def test_pointer_arguments_have_ctypes_prototypes():
+    """ctypes passes undeclared arguments as C int: a function taking a
+    pointer must have argtypes in api.load(), or its pointers get truncated."""
+    from trans_bl_gb300 import api
+    lib = api.load()
+    missing = [n for n, args in header_prototypes().items() if "*" in args and getattr(lib, n).argtypes is None]
+    assert not missing, missing
+
+
+def test_dft_matrix_sizes():
+    import numpy as np
+    from trans_bl_gb300 import api
+    for P in (16, 128):
+        Ti, Tf = api.dft_matrix(P, False), api.dft_matrix(P, True)
+        # forward after inverse is the identity on the slots the transforms keep
+        # (Re c0 is the mean, carried outside the matrices; Im c0 is dropped forward)
+        M = Tf @ Ti
+        keep = np.arange(2, P)
+        assert np.max(np.abs(M[np.ix_(keep, keep)] - np.eye(P - 2))) < 1e-12
+    with pytest.raises(api.TbError):
+        api.dft_matrix(12, False)
