@@ -680,17 +680,25 @@ int tb_learn_train(tb_ctx* c, long long n_train, int iters, int batch, float lr,
     cudaStream_t st = c->stream;
     if (L->adam_t == 0) {   // a fresh training run: input and output scales = RMS of the planes
         double* acc = tb.dloss;
-        TB_CUDA(cudaMemsetAsync(acc, 0, PLANES * sizeof(double), st));
-        k_plane_sq<<<dim3(128, PLANES), 256, 0, st>>>(L->samples, n_train, acc);
-        double sq[PLANES];
-        TB_CUDA(cudaMemcpyAsync(sq, acc, sizeof sq, cudaMemcpyDeviceToHost, st));
-        TB_CUDA(cudaStreamSynchronize(st));
+        double sq[PLANES] = {0, 0, 0, 0, 0};
+        cudaError_t e = cudaMemsetAsync(acc, 0, PLANES * sizeof(double), st);
+        if (e == cudaSuccess) {
+            k_plane_sq<<<dim3(128, PLANES), 256, 0, st>>>(L->samples, n_train, acc);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(sq, acc, sizeof sq, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         float sc[PLANES];
         for (int p = 0; p < PLANES; p++) {
             sc[p] = (float)std::sqrt(sq[p] / ((double)n_train * CROP * CROP));
             if (!(sc[p] > 0.f) || !std::isfinite(sc[p])) sc[p] = 1.f;
         }
-        TB_CUDA(cudaMemcpy(L->w + OIS, sc, sizeof sc, cudaMemcpyHostToDevice));   // OIS .. OIS + 3, then OSC
+        if (e == cudaSuccess) e = cudaMemcpy(L->w + OIS, sc, sizeof sc, cudaMemcpyHostToDevice);   // OIS .. OIS + 3, then OSC
+        if (e != cudaSuccess) {
+            tb_set_error("training: %s", cudaGetErrorString(e));
+            tb.release();
+            return TB_ERR_CUDA;
+        }
     }
     std::mt19937_64 g(seed);
     std::uniform_int_distribution<long long> pick(0, n_train - 1);
@@ -698,10 +706,17 @@ int tb_learn_train(tb_ctx* c, long long n_train, int iters, int batch, float lr,
     double acc = 0.0;
     int nacc = 0;
     const int tail = std::max(1, iters / 10);
-    TB_CUDA(cudaMemsetAsync(tb.loss, 0, sizeof(double), st));
+    if (cudaMemsetAsync(tb.loss, 0, sizeof(double), st) != cudaSuccess) {
+        tb_set_error("training: %s", cudaGetErrorString(cudaGetLastError()));
+        r = TB_ERR_CUDA;
+    }
     for (int it = 0; it < iters && !r; it++) {
         for (int b = 0; b < batch; b++) idx[b] = (int)pick(g);
-        TB_CUDA(cudaMemcpyAsync(tb.idx, idx.data(), batch * sizeof(int), cudaMemcpyHostToDevice, st));
+        if (cudaMemcpyAsync(tb.idx, idx.data(), batch * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            tb_set_error("training: %s", cudaGetErrorString(cudaGetLastError()));
+            r = TB_ERR_CUDA;
+            break;
+        }
         k_batch<<<tb_blocks((size_t)batch * PLANES * CW * CW, 256), 256, 0, st>>>(L->samples, tb.idx, tb.X, tb.T, batch,
                                                                                    L->w + OIS);
         k_meta<<<tb_blocks((size_t)3 * batch, 128), 128, 0, st>>>(L->meta, tb.idx, tb.bmeta, batch);
