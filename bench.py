@@ -145,15 +145,24 @@ def peaks():
 WORKLOAD = {"name": "config2"}
 
 
-def workload(form):
+def workload(form, make_default=None):
     from trans_bl_gb300 import api, configs
     prec = api.FORM_MIXED if form == "mixed" else api.FORM_PLAIN_FP64
+    kw = dict(tol=1e-10, precision=prec, make_default=make_default)
     if WORKLOAD["name"] == "small":
-        return configs.small(nx=129, ny=65, kfour=8, kphys=16, msh=3, tol=1e-10, precision=prec)
+        return configs.small(nx=129, ny=65, kfour=8, kphys=16, msh=3, **kw)
     if WORKLOAD["name"] == "medium":
-        return configs.blasius_ts_config(513, 193, 16, 32, 4, steps_per_period=1024, amp2d=1e-4, amp3d=1e-5,
-                                         tol=1e-10, precision=prec)
-    return configs.config2(tol=1e-10, precision=prec)
+        return configs.blasius_ts_config(513, 193, 16, 32, 4, steps_per_period=1024, amp2d=1e-4, amp3d=1e-5, **kw)
+    return configs.config2(**kw)
+
+
+def product_library_mapped():
+    """Whether this process has the GPU library mapped (Linux /proc)."""
+    try:
+        with open("/proc/self/maps") as f:
+            return any("libtransbl.so" in line for line in f)
+    except OSError:
+        return None
 
 
 def workload_name(cfg):
@@ -166,50 +175,76 @@ def start_state(cfg, base):
     return configs.disturbed_state(cfg, base, np.random.default_rng(5))
 
 
-def cpu_step_seconds(cfg, coefs, base, state, threads, t):
-    """One RK4 step (four stages, the filter in the fourth) of the oracle on
-    the given state, on `threads` host threads (s)."""
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as ora
+    return ora
+
+
+def cpu_step_seconds(cfg, coefs, base, state, threads, t, steps=1):
+    """RK4 steps (four stages, the filter in the fourth) of the oracle from
+    the given state, on `threads` host threads: seconds per step."""
+    ora = _oracle()
+    used = ora.set_threads(threads)
+    o = ora.Oracle(cfg, coefs, base)
+    o.put_state(state)
+    times = []
+    for q in range(steps):
+        t0 = time.perf_counter()
+        o.step(t + q)
+        times.append(time.perf_counter() - t0)
+    o.close()
+    return times, used
+
+
+def cpu_stage_seconds(cfg, coefs, base, state, threads, t):
+    """One RK4 stage (stage 1) of the oracle on `threads` host threads (s)."""
+    ora = _oracle()
     used = ora.set_threads(threads)
     o = ora.Oracle(cfg, coefs, base)
     o.put_state(state)
     t0 = time.perf_counter()
-    o.step(t)
+    o.rk_stage(1, t)
     el = time.perf_counter() - t0
     o.close()
     return el, used
 
 
 def run_reference(args, rank, world):
-    """Reference arm: the CPU restatement of the reference path, all host threads."""
+    """Reference arm: the CPU restatement of the reference path (the oracle)
+    on all host threads, built and fed without the GPU library: the workload's
+    coefficient tables and Falkner-Skan base flow come from the oracle's own
+    restatement of the reference's pre-processing.  W warm-up steps, then K
+    timed steps continuing the same trajectory, as the GPU arm does."""
     if rank != 0:
         return
-    from trans_bl_gb300 import configs
-    cfg = workload("plain")
-    coefs, base = configs.setup_inputs(cfg)
+    ora = _oracle()
+    ora.build()
+    cfg = workload("plain", make_default=ora.default_config)
+    coefs, base = ora.setup_inputs(cfg)
     st = start_state(cfg, base)
     threads = os.cpu_count() or 1
     pts = cfg.nx * cfg.ny * cfg.kfour
-    warm = min(args.warmup, 1)
-    steps = max(1, min(args.steps, 2))
-    used = threads
-    for _ in range(warm):
-        _, used = cpu_step_seconds(cfg, coefs, base, st, threads, cfg.stpp + 1)
-    times = []
-    for _ in range(steps):
-        el, used = cpu_step_seconds(cfg, coefs, base, st, threads, cfg.stpp + 1)
-        times.append(el)
-    ms_per_step = 1e3 * float(np.median(times))
+    warm, steps = max(3, args.warmup), max(1, args.steps)
+    times, used = cpu_step_seconds(cfg, coefs, base, st, threads, cfg.stpp + 1, warm + steps)
+    timed = times[warm:]
+    ms_per_step = 1e3 * sum(timed) / len(timed)
     value = pts / (ms_per_step * 1e-3) / 1e6
-    sample = ("one RK4 step (four stages) of the nx=1025 ny=193 K=32 workload from the benchmark's start state, "
-              "median of %d samples after %d warm-up" % (steps, warm))
+    one_s, _ = cpu_stage_seconds(cfg, coefs, base, st, 1, cfg.stpp + 1)
+    sample = ("%d RK4 steps (four stages each) of the nx=%d ny=%d K=%d workload after %d warm-up steps, "
+              "from the benchmark's start state; median step %.2f s"
+              % (steps, cfg.nx, cfg.ny, cfg.kfour, warm, float(np.median(timed))))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpt-steps/s", "n_gpus": world,
             "steps": steps, "warmup": warm, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": workload_name(cfg),
-                       "form": "reference CPU path (C++ restatement, OpenMP over lines and modes)"},
-            "cpu_baseline": {"value": value, "unit": "Mpt-steps/s", "cores": used, "kind": "port", "sample": sample},
+                       "form": "reference CPU path (C++ restatement, OpenMP over lines and modes)",
+                       "inputs": "oracle restatement of the reference pre-processing",
+                       "gpu_library_loaded": product_library_mapped()},
+            "cpu_baseline": {"value": value, "unit": "Mpt-steps/s", "cores": used, "kind": "port", "sample": sample,
+                             "single_core": {"value": pts / (4.0 * one_s) / 1e6, "unit": "Mpt-steps/s", "cores": 1,
+                                             "sample": "one RK4 stage (stage 1) on one thread, %.2f s, x4 per "
+                                                       "step" % one_s}},
             "e2e": {"value": value, "unit": "Mpt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -371,11 +406,16 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         pcfg = workload("plain")
         threads = os.cpu_count() or 1
-        cpu_s, used = cpu_step_seconds(pcfg, coefs, base, st, threads, t)
-        cpu_val = pts / cpu_s / 1e6
-        line["cpu_baseline"] = {"value": cpu_val, "unit": "Mpt-steps/s", "cores": used, "kind": "port",
-                                "sample": "one RK4 step (four stages) of the same nx=1025 ny=193 K=32 state on %d "
-                                          "host threads (%.2f s)" % (used, cpu_s)}
+        times, used = cpu_step_seconds(pcfg, coefs, base, st, threads, t, 3)
+        cpu_s = float(np.median(times))
+        one_s, _ = cpu_stage_seconds(pcfg, coefs, base, st, 1, t)
+        line["cpu_baseline"] = {"value": pts / cpu_s / 1e6, "unit": "Mpt-steps/s", "cores": used, "kind": "port",
+                                "sample": "median of 3 RK4 steps (four stages each) continuing the GPU run's "
+                                          "nx=1025 ny=193 K=32 state on %d host threads (%.2f s per step)"
+                                          % (used, cpu_s),
+                                "single_core": {"value": pts / (4.0 * one_s) / 1e6, "unit": "Mpt-steps/s",
+                                                "cores": 1, "sample": "one RK4 stage (stage 1) on one thread, "
+                                                                      "%.2f s, x4 per step" % one_s}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -58,8 +58,71 @@ def load():
     lib.ora_poisson_stats.argtypes = [P, C.POINTER(C.c_int), D]
     lib.ora_set_threads.argtypes = [C.c_int]
     lib.ora_set_threads.restype = C.c_int
+    lib.ora_generate_coefs.argtypes = [C.c_double, C.c_int, D]
+    lib.ora_generate_fp_fd.argtypes = [C.c_double, D]
+    lib.ora_fs_wall_shear.argtypes = [C.c_double, D]
+    lib.ora_baseflow_fs.argtypes = [C.POINTER(TbConfig), C.c_double, D, D, D]
     _lib = lib
     return lib
+
+
+def default_config(**kw):
+    """A tb_config with the reference's par.for constants (par.for:34-129)
+    and the given fields, built without the GPU library."""
+    from trans_bl_gb300.api import TbConfig, FORM_PLAIN_FP64
+    cfg = TbConfig()
+    d = dict(nx=129, ny=65, kfour=4, kphys=8, msh=3, my_form=0, i0=10, i1=22, i2=36, i3=100, i4=115, stpp=368,
+             max_vcycles=11, ibm=0, precision=FORM_PLAIN_FP64, les_damping=0, warm_start=1, step_graph=1,
+             Re=5.0 * 0.1 / 1.509479531e-5, dx=0.02962963, dy=0.15 / 182.0, stf=1.0, x0=1.0, alpha=0.45723605,
+             omega=2.6, beta=34.9, fac_y=1.0, alphaf=0.48, tol_stage=1e-5, tol_final=1e-6, C_s=0.032, A_plus=25.0,
+             ibm_xc=1.7, ibm_zc=0.0, ibm_h=0.0, ibm_R=1e-2 / 0.1, n_forced=1, forced_mode=[0], forced_amp=[1e-5],
+             forced_phase=[0.0])
+    d["irf"] = -0.1 * d["Re"]
+    d.update(kw)
+    for k, v in d.items():
+        if k in ("forced_mode", "forced_amp", "forced_phase"):
+            arr = getattr(cfg, k)
+            for q in range(4):
+                arr[q] = v[q] if q < len(v) else 0
+        else:
+            setattr(cfg, k, v)
+    return cfg
+
+
+def generate_coefs(stf, msh):
+    """The coefficient blob of tb_set_coefs (100 + 24 msh doubles)."""
+    blob = np.zeros(100 + 24 * msh)
+    if load().ora_generate_coefs(float(stf), int(msh), _d(blob)) != 0:
+        raise ValueError("oracle coefficient generator failed")
+    return blob
+
+
+def generate_fp_fd(stf):
+    out = np.zeros(7)
+    if load().ora_generate_fp_fd(float(stf), _d(out)) != 0:
+        raise ValueError("oracle coefficient generator failed")
+    return out
+
+
+def fs_wall_shear(beta_fs=0.0):
+    v = np.zeros(1)
+    if load().ora_fs_wall_shear(float(beta_fs), _d(v)) != 0:
+        raise ValueError("Falkner-Skan shooting failed")
+    return float(v[0])
+
+
+def baseflow_fs(cfg, beta_fs=0.0):
+    """(uxb, uyb, wzb), each (ny, nx)."""
+    shape = (cfg.ny, cfg.nx)
+    ux, uy, wz = np.zeros(shape), np.zeros(shape), np.zeros(shape)
+    if load().ora_baseflow_fs(C.byref(cfg), float(beta_fs), _d(ux), _d(uy), _d(wz)) != 0:
+        raise ValueError("Falkner-Skan base flow failed")
+    return ux, uy, wz
+
+
+def setup_inputs(cfg):
+    """Coefficient blob and Blasius base flow for cfg, from the oracle alone."""
+    return generate_coefs(cfg.stf, cfg.msh), baseflow_fs(cfg, 0.0)
 
 
 def _d(a):

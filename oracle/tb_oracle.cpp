@@ -1364,7 +1364,7 @@ void setup_delta(ora_ctx* o) {  // delta (immersed_par.f:98-181)
 extern "C" {
 
 ora_ctx* ora_create(const tb_config* cfg) {
-    if (!cfg || cfg->nx < 16 || cfg->ny < 16 || cfg->kfour < 1 || cfg->kphys < 4 || 2 * cfg->kfour > cfg->kphys + 1)
+    if (!cfg || cfg->nx < 16 || cfg->ny < 16 || cfg->kfour < 1 || cfg->kphys < 2 || 2 * cfg->kfour > cfg->kphys + 1)
         return nullptr;
     ora_ctx* o = new ora_ctx();
     o->cfg = *cfg;

@@ -70,6 +70,14 @@ int ora_poisson_stats(ora_ctx* o, int* vcycles, double* residual);
 /* Host threads of the parallel loops (n <= 0: keep); returns the count in use. */
 int ora_set_threads(int n);
 
+/* Workload inputs without the GPU library (tb_inputs.cpp): the coefficient
+ * blob of tb_set_coefs (100 + 24 msh doubles), the compact first-point weights
+ * fp_fd_coef(7), the Falkner-Skan f''(0), and the base flow as (ny, nx). */
+int ora_generate_coefs(double stf, int msh, double* blob);
+int ora_generate_fp_fd(double stf, double* out7);
+int ora_fs_wall_shear(double beta_fs, double* fpp);
+int ora_baseflow_fs(const tb_config* cfg, double beta_fs, double* uxb, double* uyb, double* wzb);
+
 #ifdef __cplusplus
 }
 #endif

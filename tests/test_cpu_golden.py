@@ -67,3 +67,32 @@ def test_blasius_profile_properties(lib_built):
     assert np.all(ux[0] == 0.0) and abs(ux[-1, 0] - 1.0) < 1e-6
     assert np.all(np.diff(ux[:, 0]) > -1e-12)
     assert np.all(wz[0] > 0)
+
+
+# The oracle's own restatement of the pre-processing (oracle/tb_inputs.cpp),
+# which builds the CPU baseline's inputs without the GPU library, against the
+# same golden data and against the library's generator.
+def test_oracle_coefficient_generator_matches_coefs_bin(oracle_built, golden):
+    blob = oracle_built.generate_coefs(1.01, 4)
+    off = 0
+    for name, n in ORDER:
+        v = blob[off:off + n]
+        off += n
+        if name == "fp_fd_e":
+            continue
+        np.testing.assert_allclose(v, np.array(golden[name]), rtol=1e-12, atol=1e-13, err_msg=name)
+    np.testing.assert_allclose(oracle_built.generate_fp_fd(1.01), golden["record1_stale_fp_fd"], rtol=1e-12)
+
+
+def test_oracle_inputs_match_library(lib_built, oracle_built):
+    from trans_bl_gb300 import api, configs
+    for stf, msh in ((1.02, 3), (1.02, 4), (1.0, 2)):
+        np.testing.assert_allclose(oracle_built.generate_coefs(stf, msh), api.generate_coefs(stf, msh),
+                                   rtol=1e-13, atol=1e-14)
+    cfg = configs.small(make_default=oracle_built.default_config)
+    assert cfg.as_dict() == configs.small().as_dict()
+    fpp = oracle_built.fs_wall_shear(0.0)
+    gold = json.load(open(os.path.join(GOLD, "fpp.json")))["fpp"][0]
+    assert abs(fpp * np.sqrt(0.5) - gold) <= 1e-13 * gold
+    for a, b in zip(oracle_built.baseflow_fs(cfg), api.baseflow_fs(cfg)):
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-14 * np.max(np.abs(b)))

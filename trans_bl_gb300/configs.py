@@ -22,8 +22,12 @@ BLASIUS_DSTAR = 1.7208  # delta* sqrt(U/(nu x)) of the Blasius profile
 def blasius_ts_config(nx, ny, kfour, kphys, msh, stf=1.02, re_dstar=1000.0, F=1e-4, n_lambda=12.0,
                       y_top_dstar=40.0, steps_per_period=256, beta_dstar=0.2, amp2d=1e-5, amp3d=0.0,
                       seed=20261203, tol=1e-10, max_vcycles=11, precision=api.FORM_PLAIN_FP64, my_form=0,
-                      strip=(3.0, 4.0)):
-    """tb_config of a flat-plate TS forcing case on an (nx, ny, kfour) grid."""
+                      strip=(3.0, 4.0), make_default=None):
+    """tb_config of a flat-plate TS forcing case on an (nx, ny, kfour) grid.
+
+    make_default(**fields) builds the tb_config from its defaults; the
+    library's tb_config_default unless given (the CPU baseline passes one that
+    does not load the library)."""
     Re = (re_dstar / BLASIUS_DSTAR) ** 2
     dstar = BLASIUS_DSTAR / math.sqrt(Re)          # at x0 = 1
     omega = F * Re                                 # F = omega nu / U^2
@@ -41,7 +45,7 @@ def blasius_ts_config(nx, ny, kfour, kphys, msh, stf=1.02, re_dstar=1000.0, F=1e
     modes, amps, phases = [0], [amp2d], [float(rng.uniform(0, 2 * math.pi))]
     if amp3d > 0 and kfour > 1:
         modes.append(1); amps.append(amp3d); phases.append(float(rng.uniform(0, 2 * math.pi)))
-    cfg = api.default_config(
+    cfg = (make_default or api.default_config)(
         nx=nx, ny=ny, kfour=kfour, kphys=kphys, msh=msh, my_form=my_form, i0=i0, i1=i1, i2=i2, i3=i3, i4=i4,
         stpp=steps_per_period, max_vcycles=max_vcycles, precision=precision,
         Re=Re, dx=dx, dy=dy0, stf=stf, x0=1.0, alpha=alpha, omega=omega, beta=beta_dstar / dstar, fac_y=1.0,
@@ -151,7 +155,7 @@ def disturbed_state(cfg, base, rng, amp=1e-3):
 
 
 def setup_inputs(cfg):
-    """Coefficient blob and Blasius base flow for cfg."""
+    """Coefficient blob and Blasius base flow for cfg (the library's generators)."""
     coefs = api.generate_coefs(cfg.stf, cfg.msh)
     base = api.baseflow_fs(cfg, 0.0)
     return coefs, base
