@@ -258,6 +258,12 @@ typedef struct tb_tune_result {
 } tb_tune_result;
 int tb_autotune(tb_ctx* ctx, tb_tune_result* out);
 
+/* No counterpart in the reference: the current device's FP64 throughput in
+   TFLOP/s (fused multiply-adds counted as two flops), measured by a short
+   kernel with CUDA events -- the denominator of the FP64-pipe rooflines the
+   benchmark reports for the FP64 kernels.  Allocates a small buffer. */
+int tb_fp64_peak(double* tflops);
+
 /* ---- ensembles: independent runs advanced together --------------------
    One recorded CUDA graph advances every member by one step: the members'
    stages run concurrently on the device and the host waits once per step.
@@ -333,13 +339,14 @@ int tb_profile_read(tb_ctx* ctx, int family, double* ms, long long* launches);
 /* No counterpart in the reference: filter_trid (filter_par.f:144) on caller
    DEVICE buffers wx, wy, wz (complex*16 (nx, ny, kfour)), for hosts that must
    not allocate GPU memory after start-up (a memory manager that owns all free
-   device memory, or a loop under stream capture).  Needs no context and
+   device memory, or a real-time section).  Needs no context and
    allocates nothing: the filtered lines are staged in a 32 MiB array built
    into the library, so one call takes nx*ny*kfour <= 2^21 - 4096 points and
    nx <= 4096 (filter larger grids one slice of Fourier modes per call) and
    returns TB_ERR_ARG beyond that.  The first call on a device sets up the
-   array's address and must precede any stream capture; calls that overlap on
-   the GPU race on the shared array.  stream is a cudaStream_t (NULL: legacy
+   array's address and must precede any stream capture (after cudaDeviceReset
+   of that device the kept address is stale: do not call it there again);
+   calls that overlap on the GPU race on the shared array.  stream is a cudaStream_t (NULL: legacy
    default stream); the call returns once the kernels are queued. */
 int tb_filter_trid_noalloc(double* wx, double* wy, double* wz, int nx, int ny, int kfour,
                            double alphaf, void* stream);

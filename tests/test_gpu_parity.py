@@ -86,17 +86,17 @@ def test_outuy(case):
     assert rel(g.get_state()["uy"], o.get_state()["uy"]) < TOL_SWEEP
 
 
-def test_poi_uy(case):
+@pytest.mark.parametrize("erro", [1e-3, 1e-10])
+def test_poi_uy(case, erro):
     g, o = pair(case)
     d = o.outuy()
     g.outuy()
-    for erro in (1e-3,):
-        g.poi_uy(d, erro)
-        o.poi_uy(d, erro)
-        assert rel(g.get_state()["uy"], o.get_state()["uy"]) < TOL_SOLVE
-        vg = g.poisson_stats()["vcycles"]
-        vo, ro = o.poisson_stats()
-        assert vg == vo, (vg, vo)
+    g.poi_uy(d, erro)
+    o.poi_uy(d, erro)
+    assert rel(g.get_state()["uy"], o.get_state()["uy"]) < TOL_SOLVE
+    vg = g.poisson_stats()["vcycles"]
+    vo, ro = o.poisson_stats()
+    assert vg == vo, (vg, vo)
 
 
 def test_poi_ux_uz(case):
@@ -163,33 +163,3 @@ def test_perturbation_parity_after_steps(case):
         da, db = a[n] - s0[n], b[n] - s0[n]
         if np.max(np.abs(db)) > 0:
             assert rel(da, db) < 1e-7, n
-
-
-def test_thousand_steps(oracle_built):
-    """The plain form against the reference CPU path over 1000 RK4 steps
-    from the initial fields (base flow, the wall forcing ramping up over the
-    first period): fields within 1e-10 relative.  The Poisson solves iterate
-    to 1e-12, so that both sides stop near the same discrete solution: at the
-    runs' 1e-10 the two iterations (which round differently) may stop one
-    V-cycle apart, and over 1000 steps the fields then differ by ~1e-9."""
-    from trans_bl_gb300 import api
-    ora = oracle_built
-    cfg, coefs, base = small_case(nx=33, ny=17, kfour=2, kphys=4, msh=3, tol=1e-12, max_vcycles=40)
-    g = api.Context(cfg, coefs, base)
-    o = ora.Oracle(cfg, coefs, base)
-    s0 = g.get_state()
-    for t in range(1, 1001):
-        g.step(t)
-        o.step(t)
-    a, b = g.get_state(), o.get_state()
-    worst, worst_d = 0.0, 0.0
-    for n in NAMES:
-        worst = max(worst, rel(a[n], b[n]))
-        db = b[n] - s0[n]
-        if np.max(np.abs(db)) > 0:
-            worst_d = max(worst_d, rel(a[n] - s0[n], db))
-    print("\n1000 steps: fields %.2e, disturbance %.2e relative" % (worst, worst_d))
-    assert worst < 1e-10
-    assert worst_d < 1e-6
-    g.close()
-    o.close()

@@ -1,0 +1,118 @@
+"""The plain FP64 form against the reference CPU path (the oracle) at the
+benchmark's grids, through the C ABI.
+
+- config 1: nx=385, ny=129, one Fourier mode (P=2), 3-level multigrid,
+  Poisson max-defect 1e-10, 256 steps per forcing period;
+- config 2: nx=1025, ny=193, 32 modes (P=64), 4-level multigrid, 1e-10.
+
+The GPU rounds differently from the oracle (fused multiply-adds, reciprocal
+pivots, a chunked scan in every line solve) but relaxes the lines in the
+reference's lexicographic order, so the multigrid iterates agree to rounding
+and the solves stop after the same number of V-cycles.
+"""
+import threading
+
+import numpy as np
+import pytest
+
+from tests.helpers import NAMES, rel
+
+pytestmark = pytest.mark.gpu
+
+
+def inputs(which, **kw):
+    from trans_bl_gb300 import api, configs
+    cfg = getattr(configs, which)(tol=1e-10, precision=api.FORM_PLAIN_FP64, **kw)
+    coefs, base = configs.setup_inputs(cfg)
+    return cfg, coefs, base
+
+
+def disturbed(cfg, base, seed):
+    from trans_bl_gb300 import configs
+    return configs.disturbed_state(cfg, base, np.random.default_rng(seed))
+
+
+@pytest.mark.parametrize("which", ["config1", "config2"])
+def test_poi_uy_at_benchmark_grids(oracle_built, which):
+    """One v-Poisson solve at tolerance 1e-10 from a disturbed state: equal
+    V-cycle counts per mode and uy within 1e-11 relative."""
+    from trans_bl_gb300 import api
+    ora = oracle_built
+    cfg, coefs, base = inputs(which)
+    st = disturbed(cfg, base, 21)
+    g = api.Context(cfg, coefs, base)
+    o = ora.Oracle(cfg, coefs, base)
+    g.put_state(st)
+    o.put_state(st)
+    d = o.outuy()
+    g.outuy()
+    g.poi_uy(d, 1e-10)
+    o.poi_uy(d, 1e-10)
+    vg = g.poisson_stats()["vcycles"][:cfg.kfour]
+    vo = o.poisson_stats()[0]
+    print("\n%s V-cycles GPU %s oracle %s" % (which, vg, vo))
+    assert vg == vo
+    assert rel(g.get_state()["uy"], o.get_state()["uy"]) < 1e-11
+    g.close()
+    o.close()
+
+
+def test_config2_step(oracle_built):
+    """One RK4 step (four stages, filter in the fourth) of config 2 from a
+    disturbed state past the forcing ramp: every field within 1e-10."""
+    from trans_bl_gb300 import api
+    ora = oracle_built
+    cfg, coefs, base = inputs("config2")
+    st = disturbed(cfg, base, 22)
+    g = api.Context(cfg, coefs, base)
+    o = ora.Oracle(cfg, coefs, base)
+    g.put_state(st)
+    o.put_state(st)
+    t = cfg.stpp + 2
+    g.step(t)
+    o.step(t)
+    a, b = g.get_state(), o.get_state()
+    errs = {n: rel(a[n], b[n]) for n in NAMES}
+    print("\nconfig 2, one step:", {n: "%.2e" % v for n, v in errs.items()})
+    for n in NAMES:
+        assert errs[n] < 1e-10, n
+    g.close()
+    o.close()
+
+
+def test_thousand_steps_config1(oracle_built):
+    """The plain form against the reference CPU path over 1000 RK4 steps of
+    config 1 from the initial fields (Blasius base flow; the wall forcing
+    ramps up over the first period): every field and the disturbance (field
+    minus initial field) within 1e-10 relative.  The oracle runs in a second
+    thread while the GPU steps."""
+    from trans_bl_gb300 import api
+    ora = oracle_built
+    cfg, coefs, base = inputs("config1")
+    g = api.Context(cfg, coefs, base)
+    o = ora.Oracle(cfg, coefs, base)
+    s0 = g.get_state()
+    nsteps = 1000
+
+    def cpu():
+        for t in range(1, nsteps + 1):
+            o.step(t)
+
+    th = threading.Thread(target=cpu)
+    th.start()
+    for t in range(1, nsteps + 1):
+        g.step(t)
+    th.join()
+    a, b = g.get_state(), o.get_state()
+    worst, worst_d = {}, {}
+    for n in NAMES:
+        worst[n] = rel(a[n], b[n])
+        db = b[n] - s0[n]
+        if np.max(np.abs(db)) > 0:
+            worst_d[n] = rel(a[n] - s0[n], db)
+    print("\n1000 steps of config 1: fields %s, disturbance %s" % (
+        {n: "%.2e" % v for n, v in worst.items()}, {n: "%.2e" % v for n, v in worst_d.items()}))
+    assert max(worst.values()) < 1e-10
+    assert max(worst_d.values()) < 1e-9
+    g.close()
+    o.close()

@@ -127,6 +127,7 @@ def load():
     lib.tb_nl_tensor_cores.argtypes = [P, C.c_int]
     lib.tb_tc_timeout_test.argtypes = [P, C.c_int]
     lib.tb_autotune.argtypes = [P, C.POINTER(TuneResult)]
+    lib.tb_fp64_peak.argtypes = [D]
     lib.tb_mixed_fp32_lines.argtypes = [P, C.c_int]
     lib.tb_dft_matrix.argtypes = [C.c_int, C.c_int, D]
     lib.tb_learn_init.argtypes = [P, C.c_ulonglong]
@@ -201,6 +202,13 @@ def learn_forward(w, x):
     out = np.zeros((n, H, W), dtype=np.float32)
     check(load().tb_learn_forward(fptr(w), fptr(x), n, H, W, fptr(out)), "tb_learn_forward")
     return out
+
+
+def fp64_peak():
+    """Measured FP64 throughput of the current device, TFLOP/s (FMA = 2 flops)."""
+    v = np.zeros(1)
+    check(load().tb_fp64_peak(dptr(v)), "tb_fp64_peak")
+    return float(v[0])
 
 
 def coef_count(msh):

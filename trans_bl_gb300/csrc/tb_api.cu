@@ -75,23 +75,14 @@ bool ready(tb_ctx* c) {
     return true;
 }
 
-double* g_phys_scratch_owner = nullptr;
-
 }  // namespace
 
-struct PhysScratch { double* p = nullptr; size_t n = 0; };
-static thread_local PhysScratch g_phys;
-
+// Device staging of one physical-space field for the tb_f_to_p / tb_p_to_f
+// mirrors: owned by the context (allocated on the context's device at first
+// use, freed by tb_destroy).
 static int phys_buf(tb_ctx* c, double** out) {
-    size_t n = tb_n2(c) * c->g.P;
-    if (g_phys.n < n) {
-        if (g_phys.p) cudaFree(g_phys.p);
-        g_phys.p = nullptr; g_phys.n = 0;
-        TB_CUDA(cudaMalloc(&g_phys.p, n * sizeof(double)));
-        g_phys.n = n;
-    }
-    *out = g_phys.p;
-    (void)g_phys_scratch_owner;
+    if (!c->phys_stage) TB_CUDA(cudaMalloc(&c->phys_stage, tb_n2(c) * c->g.P * sizeof(double)));
+    *out = c->phys_stage;
     return TB_OK;
 }
 
@@ -152,11 +143,12 @@ int tb_destroy(tb_ctx* c) {
                     c->tfil.af, c->tfil.gf, c->tfil.ibf, c->tfil.hff, c->tfil.hbf, c->tfil.pff, c->tfil.pbf, c->ty1.a, c->ty1.g, c->ty1.ib, c->tyfv.a, c->tyfv.g, c->tyfv.ib,
                     c->ty2.a, c->ty2.g, c->ty2.ib, c->ry1.w, c->ry1.off, c->ry1.cnt, c->ryfv.w, c->ryfv.off, c->ryfv.cnt,
                     c->ry2.w, c->ry2.off, c->ry2.cnt, c->px.lu, c->pfc, c->psc, c->pfct, c->pdef, c->pcarry,
-                    c->pstate, c->perr, c->pqdy2, c->pcoef, c->wcoef};
+                    c->pl_fc, c->pl_sc, c->pl_fct, c->pl_def, c->pstate, c->perr, c->pqdy2, c->pcoef, c->wcoef};
     for (void* p : ptrs) if (p) cudaFree(p);
     tb_graph_free(c);
     tb_learn_free(c);
     if (c->nl_phys) cudaFree(c->nl_phys);
+    if (c->phys_stage) cudaFree(c->phys_stage);
     if (c->dft_tc) cudaFree(c->dft_tc);
     if (c->tc_err) cudaFree(c->tc_err);
     for (int q = 0; q < 24; q++) if (c->tmp[q]) cudaFree(c->tmp[q]);
@@ -175,6 +167,7 @@ int tb_set_coefs(tb_ctx* c, const double* blob) {
     int r;
     if ((r = tb_host_build_tables(c))) return r;
     if ((r = tb_poisson_setup(c))) return r;
+    if (c->cfg.precision == TB_FORM_PLAIN_FP64 && (r = tb_plain_setup(c))) return r;
     if ((r = tb_delta_setup(c))) return r;
     if (c->cfg.precision == TB_FORM_MIXED && (r = tb_mixed_setup(c))) return r;
     c->have_coefs = true;

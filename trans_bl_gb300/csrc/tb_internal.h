@@ -105,6 +105,9 @@ struct tb_ctx {
     // Poisson work (per mode blocks of lvl_elems complex): fc, sc, fct
     cplx *pfc = nullptr, *psc = nullptr, *pfct = nullptr, *pdef = nullptr;
     double* pcarry = nullptr;    // precomputed chunk propagators of the line solve
+    // plain form: line-contiguous real/imaginary planes per (mode, part) of
+    // the multigrid arrays (element (i, j) of level l at lvl_off[l] + i*ptsy[l] + j)
+    double *pl_fc = nullptr, *pl_sc = nullptr, *pl_fct = nullptr, *pl_def = nullptr;
     int* pstate = nullptr;       // per mode: [0] active, [1] vcycles done
     double* perr = nullptr;      // per mode max|defect|
     double* pqdy2 = nullptr;     // v_qdy2 on device (ny*msh)
@@ -118,6 +121,7 @@ struct tb_ctx {
     void* mixed = nullptr;
     int ws_stage = 0, ws_t = 0;  // RK stage and step of the running loop (0: a mirror call)
     float* nl_phys = nullptr;    // mixed nlterms: FP32 physical disturbance of the 6 fields (6, P, nx*ny)
+    double* phys_stage = nullptr; // (P, nx*ny) staging of the tb_f_to_p / tb_p_to_f mirrors
     // optional CUDA-event timing of kernel families (tb_profile)
     bool prof = false;
     struct ProfRec { int id; cudaEvent_t a, b; };
@@ -198,14 +202,15 @@ int tb_poi_uz_k(tb_ctx* c, const cplx* duydy);
 int tb_wx_wall_k(tb_ctx* c, cplx* lapv);
 int tb_wz_wall_k(tb_ctx* c, const cplx* lapv);
 int tb_ts_pert_k(tb_ctx* c, int t, double tempt);
-int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro);
+int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro);   // plain FP64 form (tb_plain.cu)
+int tb_plain_setup(tb_ctx* c);
 int tb_poisson_setup(tb_ctx* c);
 int tb_poisson_begin(tb_ctx* c, const cplx* dwzdx);
 int tb_poisson_defect_f32(tb_ctx* c, float2* r32, float2* e32, size_t elems32, unsigned long long* maxsq);
 int tb_poisson_end(tb_ctx* c);
 void tb_chunk_tables(int n, int ny, int S, const double* L1, const double* L2, const double* U1, const double* U2,
                      const double* ID, double* out);
-inline size_t tb_poi_blk_size(int ny) { return (size_t)9 * ny + 1280; }
+__host__ __device__ inline size_t tb_poi_blk_size(int ny) { return (size_t)9 * ny + 1280; }
 int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro);
 // Learned first correction of the mixed solve (tb_learn.cu owns the network
 // and buffers, tb_mixed.cu the solver-side kernels).

@@ -3,11 +3,11 @@
 //
 // Some hosts cannot call cudaMalloc once their time loop runs: a Fortran
 // driver whose memory manager hands every free byte of the GPU to its own
-// pool at start-up, or a caller that brackets its loop in a stream capture
-// or a real-time section where a device allocation (which may synchronise the
-// whole device) is not allowed.  tb_filter_trid_noalloc serves them: the
-// filtered lines are staged in a fixed scratch array that lives in the
-// library's own device image instead of a per-context allocation.
+// pool at start-up, or a real-time section where a device allocation (which
+// may synchronise the whole device) is not allowed.  tb_filter_trid_noalloc
+// serves them: the filtered lines are staged in a fixed scratch array that
+// lives in the library's own device image instead of a per-context
+// allocation.
 //
 //  - Scratch: 2^21 complex*16 elements (32 MiB), a file-scope __device__
 //    array; one call filters at most nx*ny*kfour = 2^21 - 4096 points with
@@ -15,12 +15,16 @@
 //    filter treats independently).  Every GPU that loads this library keeps
 //    the array resident until the process exits.
 //  - The first call on a device (with that device current) looks up the
-//    array's device address with cudaGetSymbolAddress; make that first call
-//    before any stream capture.
+//    array's device address with cudaGetSymbolAddress and keeps it for the
+//    device; make that first call before any stream capture.  The kept
+//    address belongs to the device's primary context: after cudaDeviceReset
+//    of that device it is stale, so a process that resets a device must not
+//    call this entry point on it again.
 //  - All calls share the one array: calls that overlap on the GPU (two
 //    streams, or two host threads) race on it.  Every element the kernels read
 //    is written earlier in the same call, so nothing needs clearing.
 #include "tb_internal.h"
+#include <atomic>
 
 #define TB_NOALLOC_FILTER_MAX (1u << 21)      // complex*16 elements in the scratch (32 MiB)
 #define TB_NOALLOC_PIVOTS 4096                 // the last elements hold the Thomas pivots (nx <= 4096)
@@ -30,7 +34,9 @@ static __device__ __align__(256) double2 g_filter_scratch[TB_NOALLOC_FILTER_MAX]
 
 namespace {
 
-double2* g_scratch_addr[64] = {nullptr};
+// Device address of the scratch per device ordinal, set by the first call on
+// that device (concurrent first calls store the same value).
+std::atomic<double2*> g_scratch_addr[64];
 
 // Forward Thomas sweep of the filter LHS built on the fly (lhs_tridf
 // filter_par.f:181, quotient sequence of tridseqx derivs_par.f:1009), one
@@ -97,12 +103,14 @@ int scratch_address(double2** out) {
     int dev = 0;
     TB_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) { tb_set_error("device ordinal %d out of range", dev); return TB_ERR_ARG; }
-    if (!g_scratch_addr[dev]) {
+    double2* a = g_scratch_addr[dev].load(std::memory_order_acquire);
+    if (!a) {
         void* p = nullptr;
         TB_CUDA(cudaGetSymbolAddress(&p, g_filter_scratch));
-        g_scratch_addr[dev] = static_cast<double2*>(p);
+        a = static_cast<double2*>(p);
+        g_scratch_addr[dev].store(a, std::memory_order_release);
     }
-    *out = g_scratch_addr[dev];
+    *out = a;
     return TB_OK;
 }
 

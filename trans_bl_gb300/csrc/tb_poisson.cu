@@ -1,15 +1,9 @@
-// tb_poisson.cu -- multigrid v-Poisson per spanwise mode, plain FP64 form
-// (poi_uy and its helpers, poisson_par.f:6-963; band solves penta_par.f:308-404).
-//
-// The reference relaxes x-lines in lexicographic order (each y-line solve uses
-// the lines i-1, i-2 already updated in the same sweep), so within one mode
-// the lines are strictly sequential.  Here one CTA owns one mode and walks the
-// lines in the reference order.  Each y-line solve (a pentadiagonal LU whose
-// factors depend only on mode and level, factored once at set-up) is split
-// into 32 row chunks, one per lane: local recurrences with zero carry, a warp
-// scan of the 2x2 chunk propagators (precomputed), and a fix-up with
-// precomputed homogeneous responses.  Defect, restriction, correction and
-// interpolation are grid-parallel over all modes.
+// tb_poisson.cu -- the pieces of poi_uy (poisson_par.f:6-164) that the mixed
+// form shares: the source and start state (function_source) in the complex
+// x-contiguous work arrays, the fine-level FP64 defect of the correction
+// equation, the write-back of fc into uy, and the set-up of the y-line band
+// LU factors with their chunk tables (band5_poi, penta_par.f:308-364) used by
+// both forms.  The plain FP64 form's V-cycle is in tb_plain.cu.
 #include "tb_internal.h"
 #include <cmath>
 #include <cstring>
@@ -18,9 +12,6 @@
 
 
 namespace {
-
-constexpr int SOR_THREADS = 128;
-constexpr int SMAX = 16;  // rows per lane (ny <= 512)
 
 // Layout of one (type, level, mode) block of solve tables (doubles):
 //   [0, 5ny)          L1, L2, U1, U2, ID            (band5_poi factors)
@@ -88,155 +79,6 @@ __global__ void k_source(PoiDev P, const cplx* wx, const cplx* dwzdx, const cplx
 }
 
 // ---------------------------------------------------------------------------
-// One lexicographic line-relaxation pass set (sor, poisson_par.f:167-226).
-template <int S>
-__global__ void __launch_bounds__(SOR_THREADS) k_sor(PoiDev P, int l, int itera, double rf) {
-    int k = blockIdx.x;
-    if (!P.state[2 * k]) return;
-    const int nxl = P.ptsx[l], n = P.ptsy[l];
-    extern __shared__ cplx sm[];
-    cplx* g = sm;         // x-stencil sums per row
-    cplx* r = sm + n;     // line right-hand side
-    const double* cf = P.coef + 24 * l;
-    const double sp2 = cf[1], sp3 = cf[2], cp1 = cf[7], cp2 = cf[8], cp3 = cf[9];
-    const double qx = 1.0 / (12.0 * P.dx2[l] * P.fac_y);
-    cplx* F = P.fc + (size_t)k * P.elems + P.off[l];
-    const cplx* SC = P.sc + (size_t)k * P.elems + P.off[l];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int r0 = lane * S, r1 = min(n, r0 + S);  // lane rows [r0, r1); S = max(2, ceil(n / 32))
-    for (int it = 0; it < itera; it++) {
-        for (int step = 0; step < nxl - 2; step++) {
-            // order: border i=2, border i=nx-1, then centre 3..nx-2 (1-based)
-            int i, type;
-            if (step == 0) { i = 1; type = 1; }
-            else if (step == 1) { i = nxl - 2; type = 1; }
-            else { i = step; type = 0; }
-            // phase A: x-stencil per row
-            for (int j = threadIdx.x; j < n; j += blockDim.x) {
-                const cplx* Fj = F + (size_t)nxl * j;
-                cplx v;
-                if (type == 0) {
-                    cplx a = Fj[i - 2], b = Fj[i - 1], c = Fj[i + 1], d = Fj[i + 2];
-                    v = make_double2(16.0 * (b.x + c.x) - (a.x + d.x), 16.0 * (b.y + c.y) - (a.y + d.y));
-                } else {
-                    int e = (i == 1) ? 1 : -1;
-                    cplx a = Fj[i - e], b = Fj[i + e], c = Fj[i + 2 * e], d = Fj[i + 3 * e], f = Fj[i + 4 * e];
-                    v = make_double2(10.0 * a.x - 4.0 * b.x + 14.0 * c.x - 6.0 * d.x + f.x,
-                                     10.0 * a.y - 4.0 * b.y + 14.0 * c.y - 6.0 * d.y + f.y);
-                }
-                g[j] = v;
-            }
-            __syncthreads();
-            // phase B: rhs rows
-            for (int j = threadIdx.x; j < n; j += blockDim.x) {
-                cplx v;
-                if (j == 0) v = F[i];
-                else {
-                    cplx s = SC[(size_t)i + (size_t)nxl * j];
-                    cplx t;
-                    if (j == 1) t = make_double2(sp3 * g[2].x + sp2 * g[1].x, sp3 * g[2].y + sp2 * g[1].y);
-                    else if (j <= n - 3)
-                        t = make_double2(cp1 * g[j - 1].x + cp2 * g[j].x + cp3 * g[j + 1].x,
-                                         cp1 * g[j - 1].y + cp2 * g[j].y + cp3 * g[j + 1].y);
-                    else t = g[j];
-                    v = make_double2(s.x - qx * t.x, s.y - qx * t.y);
-                }
-                r[j] = v;
-            }
-            __syncthreads();
-            // phase C: pentadiagonal solve by warp 0, chunked over lanes
-            if (warp == 0) {
-                const double* T = P.tab + ((((size_t)type * P.msh + l) * P.K + k) * blk_size(P.ny));
-                const double *L1 = T, *L2 = T + P.ny, *U1 = T + 2 * P.ny, *U2 = T + 3 * P.ny, *ID = T + 4 * P.ny;
-                const double *h1 = T + 5 * P.ny, *h2 = T + 6 * P.ny, *k1 = T + 7 * P.ny, *k2 = T + 8 * P.ny;
-                const double* Pf = T + 9 * P.ny;
-                const double* Pb = Pf + 640;
-                cplx y[S];
-                // forward local (zero incoming)
-                cplx ym1 = make_double2(0, 0), ym2 = make_double2(0, 0);
-#pragma unroll
-                for (int s = 0; s < S; s++) {
-                    int j = r0 + s;
-                    if (j < r1) {
-                        cplx v = r[j];
-                        double a1 = L1[j], a2 = L2[j];
-                        cplx yy = make_double2(v.x - a2 * ym2.x - a1 * ym1.x, v.y - a2 * ym2.y - a1 * ym1.y);
-                        y[s] = yy; ym2 = ym1; ym1 = yy;
-                    }
-                }
-                // outgoing state (y_e, y_{e-1}) with zero incoming
-                cplx b0 = ym1, b1 = ym2;
-#pragma unroll
-                for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
-                    cplx o0, o1;
-                    o0.x = __shfl_up_sync(0xffffffffu, b0.x, off); o0.y = __shfl_up_sync(0xffffffffu, b0.y, off);
-                    o1.x = __shfl_up_sync(0xffffffffu, b1.x, off); o1.y = __shfl_up_sync(0xffffffffu, b1.y, off);
-                    if (lane >= off) {
-                        const double* M = Pf + (d * 32 + lane) * 4;
-                        b0 = make_double2(b0.x + M[0] * o0.x + M[1] * o1.x, b0.y + M[0] * o0.y + M[1] * o1.y);
-                        b1 = make_double2(b1.x + M[2] * o0.x + M[3] * o1.x, b1.y + M[2] * o0.y + M[3] * o1.y);
-                    }
-                }
-                // incoming carry from the previous lane
-                cplx Y1, Y2;
-                Y1.x = __shfl_up_sync(0xffffffffu, b0.x, 1); Y1.y = __shfl_up_sync(0xffffffffu, b0.y, 1);
-                Y2.x = __shfl_up_sync(0xffffffffu, b1.x, 1); Y2.y = __shfl_up_sync(0xffffffffu, b1.y, 1);
-                if (lane == 0) { Y1 = make_double2(0, 0); Y2 = make_double2(0, 0); }
-#pragma unroll
-                for (int s = 0; s < S; s++) {
-                    int j = r0 + s;
-                    if (j < r1) {
-                        double a = h1[j], b = h2[j];
-                        y[s] = make_double2(y[s].x + a * Y1.x + b * Y2.x, y[s].y + a * Y1.y + b * Y2.y);
-                    }
-                }
-                // backward local (zero incoming from the right)
-                cplx xp1 = make_double2(0, 0), xp2 = make_double2(0, 0);
-#pragma unroll
-                for (int s = S - 1; s >= 0; s--) {
-                    int j = r0 + s;
-                    if (j < r1) {
-                        double u1 = U1[j], u2 = U2[j], id = ID[j];
-                        cplx xx = make_double2((y[s].x - u1 * xp1.x - u2 * xp2.x) * id, (y[s].y - u1 * xp1.y - u2 * xp2.y) * id);
-                        y[s] = xx; xp2 = xp1; xp1 = xx;
-                    }
-                }
-                // outgoing (x_s, x_{s+1}); scan from high lanes to low
-                b0 = xp1; b1 = xp2;
-#pragma unroll
-                for (int d = 0, off = 1; d < 5; d++, off <<= 1) {
-                    cplx o0, o1;
-                    o0.x = __shfl_down_sync(0xffffffffu, b0.x, off); o0.y = __shfl_down_sync(0xffffffffu, b0.y, off);
-                    o1.x = __shfl_down_sync(0xffffffffu, b1.x, off); o1.y = __shfl_down_sync(0xffffffffu, b1.y, off);
-                    if (lane + off < 32) {
-                        const double* M = Pb + (d * 32 + lane) * 4;
-                        b0 = make_double2(b0.x + M[0] * o0.x + M[1] * o1.x, b0.y + M[0] * o0.y + M[1] * o1.y);
-                        b1 = make_double2(b1.x + M[2] * o0.x + M[3] * o1.x, b1.y + M[2] * o0.y + M[3] * o1.y);
-                    }
-                }
-                cplx X1, X2;
-                X1.x = __shfl_down_sync(0xffffffffu, b0.x, 1); X1.y = __shfl_down_sync(0xffffffffu, b0.y, 1);
-                X2.x = __shfl_down_sync(0xffffffffu, b1.x, 1); X2.y = __shfl_down_sync(0xffffffffu, b1.y, 1);
-                if (lane == 31) { X1 = make_double2(0, 0); X2 = make_double2(0, 0); }
-                // fix-up and relaxation fc += rf (x - fc), rows j >= 1
-#pragma unroll
-                for (int s = 0; s < S; s++) {
-                    int j = r0 + s;
-                    if (j < r1 && j >= 1) {
-                        double a = k1[j], b = k2[j];
-                        cplx xx = make_double2(y[s].x + a * X1.x + b * X2.x, y[s].y + a * X1.y + b * X2.y);
-                        cplx& f = F[(size_t)i + (size_t)nxl * j];
-                        cplx fo = f;
-                        f = make_double2(fo.x + rf * (xx.x - fo.x), fo.y + rf * (xx.y - fo.y));
-                    }
-                }
-            }
-            __syncthreads();
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
 // The level-l operator of defect (poisson_par.f:543-793) applied to fc at the
 // interior point (i, j) of mode k: L fc = den*Dxx + q2*Dyy + k2b2*ify*M - top.
 // The x-stencil sum of row jj (rhs_center / rhs_border incl. the diagonal):
@@ -301,30 +143,6 @@ __device__ __forceinline__ cplx poi_Lu_b(const PoiDev& P, int l, int k, int i, i
     return make_double2(b.x * den + cc.x * q2 + d.x * ify - top * fij.x, b.y * den + cc.y * q2 + d.y * ify - top * fij.y);
 }
 
-__device__ __forceinline__ cplx poi_Lu(const PoiDev& P, int l, int k, int i, int j) {
-    return poi_Lu_b(P, l, k, i, j, [&](int jj) { return poi_bx(P, l, k, i, jj); });
-}
-
-// defect (poisson_par.f:543-793): def = sc + si * (L fc) at level l;
-// si > 0 also stores it into sc(l) (coarse right-hand side).
-__global__ void k_defect(PoiDev P, int l, double si) {
-    const int nxl = P.ptsx[l], n = P.ptsy[l];
-    size_t per = (size_t)(nxl - 2) * (n - 1);
-    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (q >= per * P.K) return;
-    int k = (int)(q / per);
-    if (!P.state[2 * k]) return;
-    size_t rq = q % per;
-    int i = 1 + (int)(rq % (nxl - 2));
-    int j = 1 + (int)(rq / (nxl - 2));
-    cplx Lu = poi_Lu(P, l, k, i, j);
-    const cplx* SC = P.sc + (size_t)k * P.elems + P.off[l];
-    cplx s = SC[(size_t)i + (size_t)nxl * j];
-    cplx v = make_double2(s.x + si * Lu.x, s.y + si * Lu.y);
-    P.def[(size_t)k * P.dstride + (size_t)i + (size_t)nxl * j] = v;
-    if (si > 0) AT(P.sc, P, k, l, i, j) = v;
-}
-
 // Fine-level FP64 defect d = sc - L fc for the mixed form: stored as FP32 in
 // the line-contiguous right-hand side r32 of the correction equation (element
 // (i, j) of mode k at k*elems32 + i*ny + j, through a 32x32 shared tile), the
@@ -382,116 +200,6 @@ __global__ void k_defect_f32(PoiDev P, float2* r32, float2* e32, size_t elems32,
             e32[o] = make_float2(0.f, 0.f);
         }
     }
-}
-
-// get_max_value + verifica_poi (poisson_par.f:67-108, 945-963): per mode.
-__global__ void k_check(PoiDev P, double tol, int vcycle) {
-    int k = blockIdx.x;
-    if (!P.state[2 * k]) return;
-    const int nx = P.ptsx[0], n = P.ptsy[0];
-    const cplx* D = P.def + (size_t)k * P.dstride;
-    double m = 0.0;
-    int nonfinite = 0;
-    for (int q = threadIdx.x; q < (nx - 2) * (n - 1); q += blockDim.x) {
-        int i = 1 + q % (nx - 2), j = 1 + q / (nx - 2);
-        cplx v = D[(size_t)i + (size_t)nx * j];
-        double a = hypot(v.x, v.y);
-        if (!(a == a) || isinf(a)) nonfinite = 1;
-        m = fmax(m, a);
-    }
-    __shared__ double red[256];
-    __shared__ int bad;
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
-    if (nonfinite) bad = 1;
-    red[threadIdx.x] = m;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        double e = bad ? __longlong_as_double(0x7ff8000000000000LL) : red[0];
-        P.err[k] = e;
-        if (bad) { P.state[2 * k] = 0; P.state[2 * k + 1] = -1 - vcycle; }
-        else if (e < tol) { P.state[2 * k] = 0; P.state[2 * k + 1] = vcycle - 1; }
-    }
-}
-
-// restrict (poisson_par.f:796-874): level l -> l+1.
-__global__ void k_restrict(PoiDev P, int l) {
-    const int nxc = P.ptsx[l + 1], nyc = P.ptsy[l + 1], nxf = P.ptsx[l], nyf = P.ptsy[l];
-    size_t per = (size_t)nxc * nyc;
-    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (q >= per * P.K) return;
-    int k = (int)(q / per);
-    if (!P.state[2 * k]) return;
-    int i = (int)((q % per) % nxc), j = (int)((q % per) / nxc);
-    const cplx* Ff = P.fc + (size_t)k * P.elems + P.off[l];
-    const cplx* Df = P.def + (size_t)k * P.dstride;
-    auto ff = [&](int ii, int jj) { return Ff[(size_t)ii + (size_t)nxf * jj]; };
-    auto df = [&](int ii, int jj) { return Df[(size_t)ii + (size_t)nxf * jj]; };
-    int fi = 2 * i, fj = 2 * j;
-    cplx v;
-    if (j == nyc - 1) fj = nyf - 1;
-    if (i == nxc - 1) fi = nxf - 1;
-    v = ff(fi, fj);
-    AT(P.fc, P, k, l + 1, i, j) = v;
-    AT(P.fct, P, k, l + 1, i, j) = v;
-    if (i >= 1 && i <= nxc - 2) {
-        if (j >= 1 && j <= nyc - 2) {
-            cplx s = make_double2(0, 0);
-            cplx a = df(fi - 1, fj), b = df(fi + 1, fj), c = df(fi, fj - 1), d = df(fi, fj + 1), e = df(fi, fj);
-            cplx g1 = df(fi + 1, fj + 1), g2 = df(fi + 1, fj - 1), g3 = df(fi - 1, fj + 1), g4 = df(fi - 1, fj - 1);
-            s.x = 6.25e-2 * (2.0 * (a.x + b.x + c.x + d.x) + 4.0 * e.x + g1.x + g2.x + g3.x + g4.x);
-            s.y = 6.25e-2 * (2.0 * (a.y + b.y + c.y + d.y) + 4.0 * e.y + g1.y + g2.y + g3.y + g4.y);
-            AT(P.sc, P, k, l + 1, i, j) = s;
-        } else if (j == nyc - 1) {
-            cplx a = df(fi - 1, fj), e = df(fi, fj), b = df(fi + 1, fj);
-            AT(P.sc, P, k, l + 1, i, j) = make_double2(0.25 * (a.x + 2.0 * e.x + b.x), 0.25 * (a.y + 2.0 * e.y + b.y));
-        }
-    }
-}
-
-// correction (poisson_par.f:923-942) at level l (coarse).
-__global__ void k_correction(PoiDev P, int l) {
-    const int nxl = P.ptsx[l], n = P.ptsy[l];
-    size_t per = (size_t)nxl * n;
-    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (q >= per * P.K) return;
-    int k = (int)(q / per);
-    if (!P.state[2 * k]) return;
-    int i = (int)((q % per) % nxl), j = (int)((q % per) / nxl);
-    if (i < 1 || i > nxl - 2) return;
-    cplx& f = AT(P.fc, P, k, l, i, j);
-    cplx t = AT(P.fct, P, k, l, i, j);
-    f = make_double2(f.x - t.x, f.y - t.y);
-}
-
-// intpol (poisson_par.f:877-920): add the bilinear interpolant of level l to l-1.
-__global__ void k_intpol(PoiDev P, int l) {
-    const int nxc = P.ptsx[l], nxf = P.ptsx[l - 1], nyf = P.ptsy[l - 1];
-    size_t per = (size_t)nxf * nyf;
-    size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (q >= per * P.K) return;
-    int k = (int)(q / per);
-    if (!P.state[2 * k]) return;
-    int i = (int)((q % per) % nxf), j = (int)((q % per) / nxf);
-    if (i < 1 || i > nxf - 2) return;
-    const cplx* C = P.fc + (size_t)k * P.elems + P.off[l];
-    auto cv = [&](int ci, int cj) { return C[(size_t)ci + (size_t)nxc * cj]; };
-    // temp on an odd fine row (0-based even j): coarse value or x-average
-    auto row = [&](int jj) -> cplx {
-        int cj = jj / 2;
-        if ((i & 1) == 0) return cv(i / 2, cj);
-        cplx a = cv(i / 2, cj), b = cv(i / 2 + 1, cj);
-        return make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
-    };
-    cplx t;
-    if ((j & 1) == 0) t = row(j);
-    else { cplx a = row(j + 1), b = row(j - 1); t = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y)); }
-    cplx& f = AT(P.fc, P, k, l - 1, i, j);
-    f = make_double2(f.x + t.x, f.y + t.y);
 }
 
 // uy(i,j,k) = fc(i,j,1) for j >= 2, 2 <= i <= ptsx-1 (poisson_par.f:53-57).
@@ -614,94 +322,6 @@ int tb_poisson_setup(tb_ctx* c) {
     TB_CUDA(cudaMemset(c->pdef, 0, (size_t)K * c->g.nx * ny * sizeof(cplx)));
     if (!c->pstate) TB_CUDA(cudaMalloc(&c->pstate, 2 * K * sizeof(int)));
     if (!c->perr) TB_CUDA(cudaMalloc(&c->perr, K * sizeof(double)));
-    return TB_OK;
-}
-
-// poi_uy (poisson_par.f:6-64), plain FP64 form.
-int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro) {
-    PoiDev P = make_dev(c);
-    int K = c->g.K, msh = c->g.msh;
-    size_t n3 = tb_n3(c);
-    cudaEvent_t pall = nullptr;
-    if (tb_prof_begin(c, PROF_POISSON, &pall)) return TB_ERR_CUDA;
-    double stf_pow = tb_powi(c->cfg.stf, c->g.ny - 3);
-    k_source<<<tb_blocks(n3, 256), 256, 0, c->stream>>>(P, c->wx, dwzdx, c->uy, c->duexmdx, c->uyb, c->cfg.beta, c->cfg.dy,
-                                                         stf_pow, c->cfg.my_form);
-    TB_CHECK_LAUNCH(c);
-    k_activate<<<tb_blocks(K, 64), 64, 0, c->stream>>>(c->pstate, K);
-    TB_CHECK_LAUNCH(c);
-    std::vector<int> hs(2 * K);
-    int vmax = c->cfg.max_vcycles;
-    auto sor = [&](int l, int it, double rf) {
-        size_t smem = (size_t)2 * c->g.ptsy[l] * sizeof(cplx);
-        int S = std::max(2, (c->g.ptsy[l] + 31) / 32);
-        cudaEvent_t ps = nullptr;
-        if (tb_prof_begin(c, PROF_SOR, &ps)) return TB_ERR_CUDA;
-        switch (S) {
-            case 2: k_sor<2><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
-            case 3: k_sor<3><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
-            case 4: k_sor<4><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
-            case 5: k_sor<5><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
-            case 6: k_sor<6><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
-            case 7: k_sor<7><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
-            case 8: k_sor<8><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
-            case 9: k_sor<9><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
-            default: k_sor<SMAX><<<K, SOR_THREADS, smem, c->stream>>>(P, l, it, rf); break;
-        }
-        TB_CHECK_LAUNCH(c);
-        return tb_prof_end(c, PROF_SOR, ps);
-    };
-    auto defect = [&](int l, double si) {
-        size_t per = (size_t)(c->g.ptsx[l] - 2) * (c->g.ptsy[l] - 1) * K;
-        cudaEvent_t ps = nullptr;
-        if (tb_prof_begin(c, PROF_DEFECT, &ps)) return TB_ERR_CUDA;
-        k_defect<<<tb_blocks(per, 256), 256, 0, c->stream>>>(P, l, si);
-        TB_CHECK_LAUNCH(c);
-        return tb_prof_end(c, PROF_DEFECT, ps);
-    };
-    int v;
-    for (v = 1; v <= vmax; v++) {
-        for (int l = 0; l < msh - 1; l++) {
-            sor(l, 3, 1.2);
-            defect(l, -1.0);
-            if (l == 0) { k_check<<<K, 256, 0, c->stream>>>(P, erro, v); TB_CHECK_LAUNCH(c); }
-            size_t per = (size_t)c->g.ptsx[l + 1] * c->g.ptsy[l + 1] * K;
-            k_restrict<<<tb_blocks(per, 256), 256, 0, c->stream>>>(P, l); TB_CHECK_LAUNCH(c);
-            defect(l + 1, 1.0);
-        }
-        sor(msh - 1, 60, 1.2);
-        for (int l = msh - 1; l >= 1; l--) {
-            size_t per = (size_t)c->g.ptsx[l] * c->g.ptsy[l] * K;
-            k_correction<<<tb_blocks(per, 256), 256, 0, c->stream>>>(P, l); TB_CHECK_LAUNCH(c);
-            size_t perf = (size_t)c->g.ptsx[l - 1] * c->g.ptsy[l - 1] * K;
-            k_intpol<<<tb_blocks(perf, 256), 256, 0, c->stream>>>(P, l); TB_CHECK_LAUNCH(c);
-            sor(l - 1, 1, 1.0);
-        }
-        TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-        TB_CUDA(cudaStreamSynchronize(c->stream));
-        bool any = false;
-        for (int k = 0; k < K; k++) any = any || hs[2 * k];
-        if (!any) break;
-    }
-    k_write_uy<<<tb_blocks(n3, 256), 256, 0, c->stream>>>(P, c->uy);
-    TB_CHECK_LAUNCH(c);
-    if (tb_prof_end(c, PROF_POISSON, pall)) return TB_ERR_CUDA;
-    std::vector<double> he(K);
-    TB_CUDA(cudaMemcpyAsync(hs.data(), c->pstate, 2 * K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    TB_CUDA(cudaMemcpyAsync(he.data(), c->perr, K * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    TB_CUDA(cudaStreamSynchronize(c->stream));
-    c->stats.noconv = 0;
-    int nonfinite = 0;
-    for (int k = 0; k < K && k < 256; k++) {
-        int vc = hs[2 * k + 1];
-        if (hs[2 * k]) { vc = vmax; c->stats.noconv++; }
-        if (vc < 0) { nonfinite = 1; vc = -vc - 1; }
-        c->stats.vcycles[k] = vc;
-        c->stats.residual[k] = he[k];
-        c->stats.total_vcycles += vc;
-    }
-    c->stats.solves++;
-    if (nonfinite) { tb_set_error("poi_uy: non-finite defect"); return TB_ERR_NONFINITE; }
     return TB_OK;
 }
 

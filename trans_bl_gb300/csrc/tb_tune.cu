@@ -81,3 +81,55 @@ extern "C" int tb_autotune(tb_ctx* c, tb_tune_result* out) {
     TB_CUDA(cudaStreamSynchronize(c->stream));
     return tb_tc_check(c);
 }
+
+// ---------------------------------------------------------------------------
+// FP64 throughput of this GPU, measured: the denominator of the FP64-pipe
+// rooflines of the stage's FP64 kernels.  Every thread runs 8 independent
+// FMA chains (x = x * a + b, a fused multiply-add, counted as 2 flops) over
+// a grid of 8 blocks of 256 threads per SM; the time is taken with CUDA events.
+namespace {
+__global__ void k_fp64_peak(double* out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = 1.0 + 1e-3 * (threadIdx.x + q);
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) x[q] = fma(x[q], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) s += x[q];
+    out[blockIdx.x * (size_t)blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+extern "C" int tb_fp64_peak(double* tflops) {
+    if (!tflops) { tb_set_error("null argument"); return TB_ERR_ARG; }
+    int dev = 0, sms = 0;
+    TB_CUDA(cudaGetDevice(&dev));
+    TB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = 8 * sms, threads = 256, iters = 4096;
+    double* buf = nullptr;
+    TB_CUDA(cudaMalloc(&buf, (size_t)blocks * threads * sizeof(double)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_fp64_peak<<<blocks, threads>>>(buf, iters, 0.999999, 1e-7);   // warm-up
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(e0);
+        k_fp64_peak<<<blocks, threads>>>(buf, iters, 0.999999, 1e-7);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) best = ms;
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    if (e != cudaSuccess) { tb_set_error("tb_fp64_peak: %s", cudaGetErrorString(e)); return TB_ERR_CUDA; }
+    *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+    return TB_OK;
+}
