@@ -250,11 +250,17 @@ int tb_learn_op_apply(tb_ctx* ctx, int k, const float* e, float* out);
    kernels on this context's grid and keeps the fastest: warps per block of
    the x-line solves (1, 2), threads per block of the y-line solves (32, 64,
    128) and, for the mixed form with P >= 16, resident blocks per SM of the
-   tensor-core passes (1, 2, 4, 8, capped by shared and tensor memory).  It
-   touches only scratch fields.  Times are per launch of the tuned batch.  */
+   tensor-core passes (1, 2, 4, 8, capped by shared and tensor memory), and,
+   for the plain form, warps per y-line solve of the Poisson sweeps (1, 2, 4).
+   It touches only scratch fields and work arrays that every solve rebuilds.
+   Times are per launch of the tuned batch.  */
 typedef struct tb_tune_result {
     int   xline_warps, yline_threads, nl_blocks_per_sm;
     float xline_ms, yline_ms, nl_ms;
+    /* plain form: warps per y-line solve of the fine level's multi-sweep
+       (pre-smoothing) and single-sweep (post-smoothing) launches (1, 2, 4) */
+    int   plain_line_warps_multi, plain_line_warps_single;
+    float plain_multi_ms, plain_single_ms;
 } tb_tune_result;
 int tb_autotune(tb_ctx* ctx, tb_tune_result* out);
 

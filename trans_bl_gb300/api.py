@@ -58,7 +58,9 @@ class LearnStats(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("xline_warps", C.c_int), ("yline_threads", C.c_int), ("nl_blocks_per_sm", C.c_int),
-                ("xline_ms", C.c_float), ("yline_ms", C.c_float), ("nl_ms", C.c_float)]
+                ("xline_ms", C.c_float), ("yline_ms", C.c_float), ("nl_ms", C.c_float),
+                ("plain_line_warps_multi", C.c_int), ("plain_line_warps_single", C.c_int),
+                ("plain_multi_ms", C.c_float), ("plain_single_ms", C.c_float)]
 
 
 class TbError(RuntimeError):

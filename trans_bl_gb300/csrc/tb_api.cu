@@ -142,8 +142,8 @@ int tb_destroy(tb_ctx* c) {
                     c->tx2.af, c->tx2.gf, c->tx2.ibf, c->tx2.hff, c->tx2.hbf, c->tx2.pff, c->tx2.pbf,
                     c->tfil.af, c->tfil.gf, c->tfil.ibf, c->tfil.hff, c->tfil.hbf, c->tfil.pff, c->tfil.pbf, c->ty1.a, c->ty1.g, c->ty1.ib, c->tyfv.a, c->tyfv.g, c->tyfv.ib,
                     c->ty2.a, c->ty2.g, c->ty2.ib, c->ry1.w, c->ry1.off, c->ry1.cnt, c->ryfv.w, c->ryfv.off, c->ryfv.cnt,
-                    c->ry2.w, c->ry2.off, c->ry2.cnt, c->px.lu, c->pfc, c->psc, c->pfct, c->pdef, c->pcarry,
-                    c->pl_fc, c->pl_sc, c->pl_fct, c->pl_def, c->pstate, c->perr, c->pqdy2, c->pcoef, c->wcoef};
+                    c->ry2.w, c->ry2.off, c->ry2.cnt, c->px.lu, c->pfc, c->psc, c->pfct, c->pdef,
+                    c->pl_fc, c->pl_sc, c->pl_fct, c->pl_def, c->pl_tab, c->pl_maxsq, c->pstate, c->perr, c->pqdy2, c->pcoef, c->wcoef};
     for (void* p : ptrs) if (p) cudaFree(p);
     tb_graph_free(c);
     tb_learn_free(c);

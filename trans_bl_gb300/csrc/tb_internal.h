@@ -104,10 +104,11 @@ struct tb_ctx {
     PentaX px;
     // Poisson work (per mode blocks of lvl_elems complex): fc, sc, fct
     cplx *pfc = nullptr, *psc = nullptr, *pfct = nullptr, *pdef = nullptr;
-    double* pcarry = nullptr;    // precomputed chunk propagators of the line solve
     // plain form: line-contiguous real/imaginary planes per (mode, part) of
     // the multigrid arrays (element (i, j) of level l at lvl_off[l] + i*ptsy[l] + j)
     double *pl_fc = nullptr, *pl_sc = nullptr, *pl_fct = nullptr, *pl_def = nullptr;
+    double* pl_tab = nullptr;              // plain form: y-line band LU and chunk tables per line group
+    unsigned long long* pl_maxsq = nullptr;   // plain form: per mode max |defect|^2 of the fine level
     int* pstate = nullptr;       // per mode: [0] active, [1] vcycles done
     double* perr = nullptr;      // per mode max|defect|
     double* pqdy2 = nullptr;     // v_qdy2 on device (ny*msh)
@@ -154,6 +155,7 @@ struct tb_ctx {
     int tune_xw = 0;                       // warps per block of the x-line kernel (1 or 2)
     int tune_yt = 0;                       // threads per block of the y-line kernel (32, 64 or 128)
     int tune_nl = 0;                       // resident blocks per SM of the tensor-core passes
+    int tune_pg3 = 0, tune_pg1 = 0;        // plain form: 1 + log2 warps per line of multi- / single-sweep launches
 };
 
 // Kernel families timed by tb_profile (index into prof_ms / prof_n).
@@ -204,6 +206,7 @@ int tb_wz_wall_k(tb_ctx* c, const cplx* lapv);
 int tb_ts_pert_k(tb_ctx* c, int t, double tempt);
 int tb_poi_uy_k(tb_ctx* c, const cplx* dwzdx, double erro);   // plain FP64 form (tb_plain.cu)
 int tb_plain_setup(tb_ctx* c);
+int tb_plain_tune(tb_ctx* c, int l, int itera, const int* gis, int ngis, int* best, float* best_ms);
 int tb_poisson_setup(tb_ctx* c);
 int tb_poisson_begin(tb_ctx* c, const cplx* dwzdx);
 int tb_poisson_defect_f32(tb_ctx* c, float2* r32, float2* e32, size_t elems32, unsigned long long* maxsq);

@@ -13,17 +13,8 @@
 
 namespace {
 
-// Layout of one (type, level, mode) block of solve tables (doubles):
-//   [0, 5ny)          L1, L2, U1, U2, ID            (band5_poi factors)
-//   [5ny, 7ny)        h1, h2   forward homogeneous responses per row
-//   [7ny, 9ny)        k1, k2   backward homogeneous responses per row
-//   [9ny, 9ny+640)    forward scan propagators  Pf[step][lane][4]
-//   [9ny+640, +640)   backward scan propagators Pb[step][lane][4]
-__host__ __device__ inline size_t blk_size(int ny) { return (size_t)9 * ny + 1280; }
-
 struct PoiDev {
     cplx *fc, *sc, *fct, *def;    // per-mode blocks
-    const double* tab;            // solve tables
     const double* coef;           // sp(7) cp(8) pp(4) lp(5) per level
     const double* qdy2;           // (ny, msh)
     const double* k2b2;
@@ -220,7 +211,7 @@ __global__ void k_activate(int* state, int K) {
 PoiDev make_dev(tb_ctx* c) {
     PoiDev P;
     std::memset(&P, 0, sizeof P);
-    P.fc = c->pfc; P.sc = c->psc; P.fct = c->pfct; P.def = c->pdef; P.tab = c->pcarry; P.coef = c->pcoef;
+    P.fc = c->pfc; P.sc = c->psc; P.fct = c->pfct; P.def = c->pdef; P.coef = c->pcoef;
     P.qdy2 = c->pqdy2; P.k2b2 = c->k2b2; P.state = c->pstate; P.err = c->perr;
     P.nx = c->g.nx; P.ny = c->g.ny; P.K = c->g.K; P.msh = c->g.msh;
     for (int l = 0; l < c->g.msh; l++) {
@@ -295,22 +286,7 @@ void tb_chunk_tables(int n, int ny, int S, const double* L1, const double* L2, c
 
 
 int tb_poisson_setup(tb_ctx* c) {
-    int ny = c->g.ny, K = c->g.K, msh = c->g.msh;
-    size_t bs = blk_size(ny);
-    std::vector<double> all((size_t)2 * msh * K * bs, 0.0), a;
-    for (int type = 0; type < 2; type++)
-        for (int l = 0; l < msh; l++)
-            for (int k = 0; k < K; k++) {
-                tb_poisson_band_matrix(c, type, l + 1, k + 1, a);
-                int n = c->g.ptsy[l];
-                double* T = &all[(((size_t)type * msh + l) * K + k) * bs];
-                tb_band5_factor(n, a, T, T + ny, T + 2 * ny, T + 3 * ny, T + 4 * ny);
-                tb_chunk_tables(n, ny, std::max(2, (n + 31) / 32), T, T + ny, T + 2 * ny, T + 3 * ny, T + 4 * ny,
-                                T + 5 * ny);
-            }
-    if (c->pcarry) cudaFree(c->pcarry);
-    TB_CUDA(cudaMalloc(&c->pcarry, all.size() * sizeof(double)));
-    TB_CUDA(cudaMemcpy(c->pcarry, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
+    int ny = c->g.ny, K = c->g.K;
     size_t w = (size_t)K * c->g.lvl_elems;
     for (cplx** p : {&c->pfc, &c->psc, &c->pfct}) {
         if (*p) cudaFree(*p);

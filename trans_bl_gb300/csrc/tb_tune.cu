@@ -76,6 +76,16 @@ extern "C" int tb_autotune(tb_ctx* c, tb_tune_result* out) {
                       &out->nl_blocks_per_sm, &out->nl_ms)))
             return r;
     }
+    if (c->cfg.precision == TB_FORM_PLAIN_FP64 && c->pl_fc) {
+        // warps per line of the plain form's fine-level sweeps (the solve
+        // rebuilds its work arrays from uy, so the timed sweeps change nothing)
+        const int multi[3] = {0, 1, 2}, single[2] = {1, 2};
+        int b3 = 0, b1 = 0;
+        if ((r = tb_plain_tune(c, 0, 3, multi, 3, &b3, &out->plain_multi_ms))) return r;
+        if ((r = tb_plain_tune(c, 0, 1, single, 2, &b1, &out->plain_single_ms))) return r;
+        out->plain_line_warps_multi = 1 << b3;
+        out->plain_line_warps_single = 1 << b1;
+    }
     c->launches = l0;   // tuning launches are not the run's work
     tb_graph_reset(c);
     TB_CUDA(cudaStreamSynchronize(c->stream));
