@@ -45,8 +45,9 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--form", default="mixed", choices=["mixed", "plain"],
                    help="mixed: FP32 multigrid inside FP64 defect correction (default); plain: the reference's FP64 SOR")
-    p.add_argument("--workload", default="config2", choices=["config2", "medium", "small"],
-                   help="medium: 513x193x16, small: 129x65x8 grids for profiler captures")
+    p.add_argument("--workload", default="config2", choices=["config2", "config5", "medium", "small"],
+                   help="config5: 2049x257x64 with LES and a roughness element; medium: 513x193x16, small: "
+                        "129x65x8 grids for profiler captures")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
@@ -153,6 +154,8 @@ def workload(form, make_default=None):
         return configs.small(nx=129, ny=65, kfour=8, kphys=16, msh=3, **kw)
     if WORKLOAD["name"] == "medium":
         return configs.blasius_ts_config(513, 193, 16, 32, 4, steps_per_period=1024, amp2d=1e-4, amp3d=1e-5, **kw)
+    if WORKLOAD["name"] == "config5":
+        return configs.config5(**kw)
     return configs.config2(**kw)
 
 
@@ -166,8 +169,13 @@ def product_library_mapped():
 
 
 def workload_name(cfg):
-    return "blasius_ts_3d nx=%d ny=%d kfour=%d kphys=%d msh=%d tol=1e-10 steps_per_period=%d" % (
+    name = "blasius_ts_3d nx=%d ny=%d kfour=%d kphys=%d msh=%d tol=1e-10 steps_per_period=%d" % (
         cfg.nx, cfg.ny, cfg.kfour, cfg.kphys, cfg.msh, cfg.stpp)
+    if cfg.my_form == 4:
+        name += " les C_s=%g A+=%g" % (cfg.C_s, cfg.A_plus)
+    if cfg.ibm:
+        name += " roughness h=%.3g R=%.3g at x=%.3g irf=%.4g" % (cfg.ibm_h, cfg.ibm_R, cfg.ibm_xc, cfg.irf)
+    return name
 
 
 def start_state(cfg, base):
@@ -282,6 +290,7 @@ def plain_comparison(coefs, base, mixed_state2, t0, hbm_peak):
     from trans_bl_gb300 import api
     cfg = workload("plain")
     ctx = api.Context(cfg, coefs, base)
+    tune = ctx.autotune()
     ctx.put_state(start_state(cfg, base))
     ms1 = timed_steps(ctx, t0, 1)
     nv1 = np.mean(ctx.poisson_stats()["vcycles"][:cfg.kfour])
@@ -289,6 +298,7 @@ def plain_comparison(coefs, base, mixed_state2, t0, hbm_peak):
     nv2 = np.mean(ctx.poisson_stats()["vcycles"][:cfg.kfour])
     sp = ctx.get_state()
     err = {n: float(np.max(np.abs(mixed_state2[n] - sp[n])) / max(np.max(np.abs(sp[n])), 1e-300)) for n in NAMES}
+    amp = disturbance_amplitude_error(mixed_state2, sp, base)
     ctx.close()
     pts = cfg.nx * cfg.ny * cfg.kfour
     ms = min(ms1, ms2)
@@ -296,12 +306,32 @@ def plain_comparison(coefs, base, mixed_state2, t0, hbm_peak):
     value = pts / (ms * 1e-3) / 1e6
     B = step_bytes_model(nv)
     return {"value": value, "unit": "Mpt-steps/s", "ms_per_step": ms, "steps": 2,
+            "line_warps": {k: tune[k] for k in ("plain_line_warps_multi", "plain_line_warps_single")},
             "mean_vcycles_per_mode_last_solve": nv,
             "step_bytes_per_point_model": B,
             "step_roofline": {"bound": "hbm", "achieved": value * 1e6 * B / 1e9, "peak": hbm_peak, "unit": "GB/s",
                               "frac": value * 1e6 * B / 1e9 / hbm_peak},
             "mixed_vs_plain_rel_err_after_2_steps": err,
-            "max_rel_err": max(err.values())}
+            "max_rel_err": max(err.values()),
+            "disturbance_amplitude_rel_err": amp}
+
+
+def disturbance_amplitude_error(a, b, base):
+    """Relative error of the disturbance amplitude A(x) = max_y |u'(x, y)| of
+    states a against b, for ux and uy in mode 0 (2D, u' = u - base flow) and
+    mode 1 (the oblique pair): max_x |A_a - A_b| / max_x A_b, and the worst
+    of the four."""
+    out = {}
+    for n, bf in (("ux", base[0]), ("uy", base[1])):
+        for k in (0, 1):
+            if a[n].shape[0] <= k:
+                continue
+            da = a[n][k] - (bf if k == 0 else 0.0)
+            db = b[n][k] - (bf if k == 0 else 0.0)
+            Aa, Ab = np.max(np.abs(da), axis=0), np.max(np.abs(db), axis=0)
+            out["%s_mode%d" % (n, k)] = float(np.max(np.abs(Aa - Ab)) / max(np.max(Ab), 1e-300))
+    out["max"] = max(out.values())
+    return out
 
 
 def main():
@@ -358,10 +388,20 @@ def main():
     hbm_peak, peak_kind = peaks()
     stats = ctx.poisson_stats()
     if form == "plain":
-        # line-SOR: per point and sweep, read fc and sc, write fc (3 x 16 B)
-        bytes_per_launch = 48.0 * sor_points_per_launch(cfg)
+        # the lexicographic line sweeps are bound by the FP64 pipe: the
+        # reference's arithmetic per complex point and sweep (sor,
+        # poisson_par.f:167-226) is 48 flops (rhs_center 12, banbk5 forward 4
+        # and backward 5, relaxation 3; per real part 24), against the FP64
+        # throughput measured on this GPU
+        fp64 = api.fp64_peak()
+        flops = 48.0 * sor_points_per_launch(cfg)
         r_ms, r_n = fam["sor"]
-        kernel = "k_sor (lexicographic y-line SOR, one CTA per mode)"
+        achieved = flops / (r_ms * 1e-3 / max(r_n, 1)) / 1e12 if r_n else 0.0
+        roof = {"bound": "fp64", "achieved": achieved, "peak": fp64, "unit": "TFLOP/s", "frac": achieved / fp64,
+                "traffic": None, "peak_source": "measured in this run (tb_fp64_peak: FMA chains, 2 flops each)",
+                "kernel": "k_wsor (wavefront of lexicographic y-line sweeps, one CTA per mode and part)",
+                "algorithmic_flops_per_call": flops, "kernel_ms_total": r_ms, "kernel_calls": r_n,
+                "share_of_step": r_ms / prof_ms if prof_ms > 0 else None}
     else:
         # finest-level coloured y-line relaxation, FP32 complex (8 B): per
         # sweep (4 launches) every interior point reads r once, writes e once
@@ -369,16 +409,16 @@ def main():
         bytes_per_launch = 32.0 * cfg.kfour * cfg.ny * (cfg.nx - 2) / 4.0
         r_ms, r_n = fam["relax0"]
         kernel = "k_relax (finest level, one warp per y-line and mode)"
-    achieved = bytes_per_launch / (r_ms * 1e-3 / max(r_n, 1)) / 1e9 if r_n else 0.0
-    # DRAM bytes (read + write) per launch from an ncu capture of this command:
-    # the centre-colour launches of the 513-point level read 1.07x their
-    # algorithmic bytes and write none back while running; scaled by lines to
-    # the finest level of the config-2 workload
-    traffic = 1.07 * bytes_per_launch if (form == "mixed" and WORKLOAD["name"] == "config2") else None
-    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-            "traffic": traffic, "peak_source": peak_kind, "kernel": kernel,
-            "algorithmic_bytes_per_launch": bytes_per_launch, "kernel_ms_total": r_ms, "kernel_launches": r_n,
-            "share_of_step": r_ms / prof_ms if prof_ms > 0 else None}
+        achieved = bytes_per_launch / (r_ms * 1e-3 / max(r_n, 1)) / 1e9 if r_n else 0.0
+        # DRAM bytes (read + write) per launch from an ncu capture of this command:
+        # the centre-colour launches of the 513-point level read 1.07x their
+        # algorithmic bytes and write none back while running; scaled by lines to
+        # the finest level of the config-2 workload
+        traffic = 1.07 * bytes_per_launch if WORKLOAD["name"] == "config2" else None
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": traffic, "peak_source": peak_kind, "kernel": kernel,
+                "algorithmic_bytes_per_launch": bytes_per_launch, "kernel_ms_total": r_ms, "kernel_launches": r_n,
+                "share_of_step": r_ms / prof_ms if prof_ms > 0 else None}
     line = {"metric": METRIC, "value": value, "unit": "Mpt-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == "plain" else "f64+f32",
@@ -388,7 +428,9 @@ def main():
                        "step": "replayed CUDA graph" if (cfg.step_graph and form == "mixed") else "host-launched kernels",
                        "l2": "inputs larger than L2: working set ~5 GB vs 129 MB L2",
                        "start": "disturbed state (1e-3) past the forcing ramp",
-                       "launch_shapes": {k: tune[k] for k in ("xline_warps", "yline_threads", "nl_blocks_per_sm")},
+                       "launch_shapes": {k: tune[k] for k in ("xline_warps", "yline_threads", "nl_blocks_per_sm",
+                                                              "plain_line_warps_multi", "plain_line_warps_single")
+                                         if k in tune},
                        "iterations_per_mode_last_solve": float(np.mean(stats["vcycles"][:cfg.kfour]))},
             "roofline": roof, "gpu_launches": launches,
             "breakdown_ms": dict({f: v[0] for f, v in fam.items()}, profiled_steps=prof_steps, profiled_total=prof_ms),

@@ -63,8 +63,10 @@ typedef struct tb_config {
     int    les_damping; /* 0: reference cubic damping, 1: van Driest [1-e^{-y+/A}]^2*/
     int    warm_start;  /* mixed form: 1 starts each stage's v-Poisson solve from the
                            extrapolation 2 v(t-1) - v(t-2) of the same stage's solutions
-                           of the two previous steps; 0 from the current v, as the
-                           reference (no effect on the plain form)                  */
+                           of the two previous steps; 2 from the current v plus the
+                           increment between the same two stages' solutions one step
+                           earlier; 0 from the current v, as the reference (no effect
+                           on the plain form)                                       */
     int    step_graph;  /* mixed form: 1 runs tb_step/tb_steps as a recorded CUDA graph,
                            each Poisson correction loop a device-side WHILE loop, so a
                            step has no host synchronisation inside; 0 launches every

@@ -75,6 +75,40 @@ def config2(**kw):
     return blasius_ts_config(1025, 193, 32, 64, 4, **kw)
 
 
+def config5(**kw):
+    """Large 3D run with a roughness element and LES: nx=2049, ny=257 (1.02
+    stretching to 40 delta*), 64 modes (P=128), 4-level multigrid; 2D TS wave
+    plus the oblique pair at amplitude 3e-3; Smagorinsky LES (drv_les,
+    les_par.f:6-211) with C_s = 0.1 and van Driest damping A+ = 26; and the
+    reference's immersed-boundary roughness element (delta/cvirt,
+    immersed_par.f:98-313): an edge-smoothed cylinder of height 0.5 delta* and
+    diameter 2 delta* centred at 25% of the domain length (the 0.5 delta*
+    high, 2 delta* wide bump).  The steps per period keep the explicit viscous
+    term stable (as config 2): the first cell of the 257-point grid is
+    0.005 delta*, which takes 16384 steps per forcing period.  The
+    immersed-boundary gain is the reference's -0.1 Re (par.for:123), capped
+    at |irf| dt = 2 for explicit RK4 stability (|irf| dt = 0.38 at this step,
+    so the cap does not act)."""
+    kw.setdefault("amp2d", 3e-3)
+    kw.setdefault("amp3d", 3e-3)
+    kw.setdefault("my_form", 4)
+    cfg = blasius_ts_config(2049, 257, 64, 128, 4, **kw)
+    if "steps_per_period" not in kw:
+        cfg.stpp = stable_steps_per_period(cfg)
+    dstar = BLASIUS_DSTAR / math.sqrt(cfg.Re)
+    cfg.ibm = 1
+    cfg.ibm_xc = cfg.x0 + 0.25 * (cfg.nx - 1) * cfg.dx
+    cfg.ibm_zc = math.pi / cfg.beta          # mid-span
+    cfg.ibm_h = 0.5 * dstar
+    cfg.ibm_R = 1.0 * dstar
+    dt = 2.0 * math.pi / cfg.omega / cfg.stpp
+    cfg.irf = -min(0.1 * cfg.Re, 2.0 / dt)
+    cfg.C_s = 0.1
+    cfg.A_plus = 26.0
+    cfg.les_damping = 1
+    return cfg
+
+
 def stable_steps_per_period(cfg, limit=1.3):
     """Smallest power of two (>= 256) of steps per forcing period keeping the
     explicit RK4 viscous term at nu dt lambda_max <= limit, lambda_max =

@@ -459,6 +459,33 @@ __global__ void k_extrap(cplx* fc, size_t elems64, cplx* h0, cplx* h1, const int
     if (shift) h1[q] = a;
 }
 
+// warm_start = 2: the previous solve's solution fc (stage p = s - 1 of this
+// step, or stage 4 of the last step for s = 1) plus the increment between
+// the same two solves one step earlier, fc + v_s(n-1) - v_p(n-1), from this
+// stage's newest history entry h0 and stage p's older one hp1.  Stages 2 and 4
+// solve at the same time as the stage before them, so the increment is the
+// difference of two RK stage estimates and changes by O(dt^3) per step;
+// stages 1 and 3 carry half a step of time change, O(dt^2) with half the
+// constant of the linear extrapolation.  Needs one entry of this stage's
+// history and two of stage p's; shifts this stage's history as k_extrap.
+__global__ void k_extrap_inc(cplx* fc, size_t elems64, cplx* h0, cplx* h1, const cplx* hp1, const int* valid,
+                             const int* valid_p, int nx, int ny, int K, int shift) {
+    const int nv = *valid, np = *valid_p;
+    if (nv == 0) return;
+    const size_t per = (size_t)nx * ny;
+    const size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= per * K) return;
+    const int k = (int)(q / per);
+    const int i = (int)((q % per) % nx), j = (int)((q % per) / nx);
+    const cplx a = h0[q];
+    if (np >= 2 && i >= 1 && i <= nx - 2 && j >= 1) {
+        cplx& f = fc[(size_t)k * elems64 + (q % per)];
+        const cplx b = hp1[q];
+        f = make_double2(f.x + (a.x - b.x), f.y + (a.y - b.y));
+    }
+    if (shift) h1[q] = a;
+}
+
 // ---- learned first correction (network and training in tb_learn.cu) -------
 // Per mode maxima over both parts of |v1| and |v1 - v2| (history,
 // x-contiguous) and of |D^-1 d0| (d0: the FP32 copy r of the FP64 defect of
@@ -1213,8 +1240,16 @@ int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
             mx->hv_host[ws] = 0;
         }
         hv = mx->hv_host[ws];
-        k_extrap<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(c->pfc, c->g.lvl_elems, mx->hist[ws][0],
-                                                                  mx->hist[ws][1], mx->hvalid + ws, nx, ny, K, L ? 0 : 1);
+        if (c->cfg.warm_start == 2) {
+            const int p = (ws + 3) % 4;
+            k_extrap_inc<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(
+                c->pfc, c->g.lvl_elems, mx->hist[ws][0], mx->hist[ws][1], mx->hist[p][1], mx->hvalid + ws,
+                mx->hvalid + p, nx, ny, K, L ? 0 : 1);
+        } else {
+            k_extrap<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(c->pfc, c->g.lvl_elems, mx->hist[ws][0],
+                                                                      mx->hist[ws][1], mx->hvalid + ws, nx, ny, K,
+                                                                      L ? 0 : 1);
+        }
         TB_CHECK_LAUNCH(c);
         if (L && (r = learned_first(c, M, ws, L))) return r;
     }

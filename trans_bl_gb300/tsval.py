@@ -55,10 +55,11 @@ def y_coordinates(cfg):
     return cfg.dy * (cfg.stf ** j - 1.0) / (cfg.stf - 1.0)
 
 
-def lst_growth(cfg, steps=1000):
+def lst_growth(cfg, steps=1000, with_alpha=False):
     """LST growth rate at the stations x = x0 + i dx of a run of cfg (2D
     wave, Blasius wall shear), in units of the run; starts from the
-    reference's namelist point of lst_ts/ose3d.in."""
+    reference's namelist point of lst_ts/ose3d.in.  with_alpha: also the
+    streamwise wavenumber alpha_r in the same units."""
     rein = np.sqrt(cfg.Re * cfg.x0)
     w0in = 2.6134e-2
     w_target = cfg.omega / cfg.Re * rein
@@ -66,7 +67,10 @@ def lst_growth(cfg, steps=1000):
     omega_dns = w0in + (w_target - w0in) / ((steps - 1.0) / steps)
     out = api.lst_march(751.50, w0in, complex(0.08658, 1.9598e-5), rein, omega_dns, 0.0, cfg.nx, cfg.dx / cfg.x0,
                         0.33205733621540984, steps=steps)
-    return cfg.x0 * out["x"], -out["alpha"].imag * cfg.Re / out["re0"]
+    x, sigma = cfg.x0 * out["x"], -out["alpha"].imag * cfg.Re / out["re0"]
+    if with_alpha:
+        return x, sigma, out["alpha"].real * cfg.Re / out["re0"]
+    return x, sigma
 
 
 def amplitude_along_x(ctx, cfg, base_ux, t0, periods, n_snap=16):
