@@ -72,7 +72,7 @@ def default_config(**kw):
     from trans_bl_gb300.api import TbConfig, FORM_PLAIN_FP64
     cfg = TbConfig()
     d = dict(nx=129, ny=65, kfour=4, kphys=8, msh=3, my_form=0, i0=10, i1=22, i2=36, i3=100, i4=115, stpp=368,
-             max_vcycles=11, ibm=0, precision=FORM_PLAIN_FP64, les_damping=0, warm_start=1, step_graph=1,
+             max_vcycles=11, ibm=0, precision=FORM_PLAIN_FP64, les_damping=0, warm_start=2, step_graph=1,
              Re=5.0 * 0.1 / 1.509479531e-5, dx=0.02962963, dy=0.15 / 182.0, stf=1.0, x0=1.0, alpha=0.45723605,
              omega=2.6, beta=34.9, fac_y=1.0, alphaf=0.48, tol_stage=1e-5, tol_final=1e-6, C_s=0.032, A_plus=25.0,
              ibm_xc=1.7, ibm_zc=0.0, ibm_h=0.0, ibm_R=1e-2 / 0.1, n_forced=1, forced_mode=[0], forced_amp=[1e-5],

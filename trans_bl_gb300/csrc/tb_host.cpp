@@ -36,7 +36,7 @@ extern "C" int tb_config_default(tb_config* c) {
     c->nx = 129; c->ny = 65; c->kfour = 4; c->kphys = 8; c->msh = 3; c->my_form = 0;
     c->i0 = 10; c->i1 = 22; c->i2 = 36; c->i3 = 100; c->i4 = 115;
     c->stpp = 368; c->max_vcycles = 11; c->ibm = 0; c->precision = TB_FORM_PLAIN_FP64;
-    c->les_damping = 0; c->warm_start = 1; c->step_graph = 1;
+    c->les_damping = 0; c->warm_start = 2; c->step_graph = 1;
     c->Re = 5.0 * 0.1 / 1.509479531e-5;
     c->dx = 0.02962963; c->dy = 0.15 / 182.0; c->stf = 1.0; c->x0 = 1.0;
     c->alpha = 0.45723605; c->omega = 2.6; c->beta = 34.9; c->fac_y = 1.0; c->alphaf = 0.48;

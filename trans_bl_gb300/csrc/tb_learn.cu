@@ -625,7 +625,7 @@ int tb_learn_enable(tb_ctx* c, int on) {
     if (!c) { tb_set_error("null context"); return TB_ERR_ARG; }
     int r = ensure(c);
     if (r) return r;
-    if (!c->cfg.warm_start) { tb_set_error("the learned correction needs warm_start = 1"); return TB_ERR_STATE; }
+    if (!c->cfg.warm_start) { tb_set_error("the learned correction needs a warm start (warm_start > 0)"); return TB_ERR_STATE; }
     Learn* L = get(c);
     if (on) {
         const size_t hid = (size_t)2 * c->g.K * LC * c->g.nx * c->g.ny;
@@ -648,7 +648,7 @@ int tb_learn_sample(tb_ctx* c, long long capacity, int crops_per_solve, unsigned
         L->s.sample = false;
         return TB_OK;
     }
-    if (!c->cfg.warm_start) { tb_set_error("sampling needs warm_start = 1"); return TB_ERR_STATE; }
+    if (!c->cfg.warm_start) { tb_set_error("sampling needs a warm start (warm_start > 0)"); return TB_ERR_STATE; }
     if (crops_per_solve < 1) { tb_set_error("crops_per_solve must be >= 1"); return TB_ERR_ARG; }
     if (L->samples) cudaFree(L->samples);
     if (L->meta) cudaFree(L->meta);
