@@ -214,13 +214,19 @@ typedef struct tb_learn_stats {
     long long tried;       /* mode-solves that evaluated the network            */
     long long kept;        /* of those, corrections kept (the rest fell back)   */
     double    loss;        /* mean training loss over the last tenth of training */
+    long long solves;      /* gated mode: solves that passed the gate           */
+    long long evaluated;   /* gated mode: of those, solves that ran the network */
 } tb_learn_stats;
 int tb_learn_param_count(void);                 /* floats in a weight vector        */
 int tb_learn_crop_size(void);                   /* edge of a training crop (72)     */
 int tb_learn_init(tb_ctx* ctx, unsigned long long seed);   /* He-normal, last layer 0 */
 int tb_learn_set_weights(tb_ctx* ctx, const float* w);
 int tb_learn_get_weights(tb_ctx* ctx, float* w);
-int tb_learn_enable(tb_ctx* ctx, int on);       /* apply the network in every solve */
+/* on = 1: run the network in every solve; on = 2 (gated): a stage runs it
+   in the solve after one where it kept a correction for some mode, and
+   otherwise once every 16 solves, falling back to the guess without running
+   it in between; 0: off.                                                   */
+int tb_learn_enable(tb_ctx* ctx, int on);
 /* Collect crops_per_solve crops from every solve into a buffer of `capacity`
    crops; capacity 0 stops collecting and keeps the crops for training.     */
 int tb_learn_sample(tb_ctx* ctx, long long capacity, int crops_per_solve, unsigned long long seed);

@@ -53,7 +53,7 @@ class LstConfig(C.Structure):
 
 class LearnStats(C.Structure):
     _fields_ = [("samples", C.c_longlong), ("capacity", C.c_longlong), ("tried", C.c_longlong),
-                ("kept", C.c_longlong), ("loss", C.c_double)]
+                ("kept", C.c_longlong), ("loss", C.c_double), ("solves", C.c_longlong), ("evaluated", C.c_longlong)]
 
 
 class TuneResult(C.Structure):
@@ -380,8 +380,11 @@ class Context:
             raise ValueError("expected %d weights" % learn_param_count())
         self._c(self.lib.tb_learn_set_weights(self.h, fptr(w)), "tb_learn_set_weights")
 
-    def learn_enable(self, on=True):
-        self._c(self.lib.tb_learn_enable(self.h, 1 if on else 0), "tb_learn_enable")
+    def learn_enable(self, on=True, gated=False):
+        """Apply the learned correction in every solve (on), or gated: only in
+        the solve after one where it helped and once every 16 solves (gated)."""
+        mode = (2 if gated else 1) if on else 0
+        self._c(self.lib.tb_learn_enable(self.h, mode), "tb_learn_enable")
 
     def learn_sample(self, capacity, crops_per_solve=16, seed=1):
         self._c(self.lib.tb_learn_sample(self.h, int(capacity), int(crops_per_solve), seed), "tb_learn_sample")

@@ -42,10 +42,12 @@ bool graph_form(const tb_ctx* c) { return c->cfg.precision == TB_FORM_MIXED && c
 int record(tb_ctx* c) {
     const long long l0 = c->launches;
     for (long long& b : c->g_body) b = 0;
+    for (long long& b : c->g_learn) b = 0;
     c->capturing = true;
     int r = tb_graph_record_step(c);
     c->capturing = false;
-    const long long body = c->g_body[0] + c->g_body[1] + c->g_body[2] + c->g_body[3];
+    const long long body = c->g_body[0] + c->g_body[1] + c->g_body[2] + c->g_body[3] + c->g_learn[0] + c->g_learn[1] +
+                           c->g_learn[2] + c->g_learn[3];
     c->g_outer = (c->launches - l0) - body;
     c->launches = l0;
     return r;
@@ -105,6 +107,16 @@ int read_back(tb_ctx* c, const int* hs, const double* he) {
         n += c->g_body[s] * iters;
         int r = tb_mixed_absorb_stats(c, h, he + (size_t)K * s);
         if (r && !rc) rc = r;
+    }
+    // the learned correction's kernels ran in the replays whose gate opened
+    LearnSolve* L = tb_learn_solve(c);
+    if (L && L->gated && L->gate) {
+        int g[16];
+        if (cudaMemcpy(g, L->gate, sizeof g, cudaMemcpyDeviceToHost) == cudaSuccess)
+            for (int s = 0; s < 4; s++) {
+                n += c->g_learn[s] * (g[4 * s + 2] - c->g_learn_seen[s]);
+                c->g_learn_seen[s] = g[4 * s + 2];
+            }
     }
     c->launches += n;
     return rc;

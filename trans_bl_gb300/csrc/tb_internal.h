@@ -141,6 +141,8 @@ struct tb_ctx {
     double* gerr = nullptr;                // (4, K) perr after each stage's solve
     long long g_outer = 0;                 // kernels of the graph outside the WHILE bodies
     long long g_body[4] = {0, 0, 0, 0};    // kernels of one body iteration per stage
+    long long g_learn[4] = {0, 0, 0, 0};   // kernels of the learned correction's IF body per stage
+    int g_learn_seen[4] = {0, 0, 0, 0};    // network evaluations per stage counted so far
     int g_stage = 0;                       // stage being recorded (1..4)
     long long graph_gen = 0;               // bumped whenever recorded graphs go stale
     void* learn = nullptr;                 // learned first correction (tb_learn.cu)
@@ -228,6 +230,11 @@ struct LearnSolve {
     float* mfeat = nullptr;      // (K, ny) share of k^2 beta^2 in the diagonal
     cplx* g0 = nullptr;          // guess before any correction (while sampling)
     long long* tally = nullptr;  // (K, 2) solves tried / corrections kept per mode
+    // gated evaluation (tb_learn_enable mode 2): per stage [since last
+    // evaluation, modes kept at it, evaluations, solves]
+    int gated = 0;
+    int probe = 16;              // a stage evaluates the network at least every `probe` solves
+    int* gate = nullptr;         // (4, 4)
 };
 // The fine-level FP32 operator of the mixed form (the operator of k_resid at
 // level 0): device tables and scalars.

@@ -577,7 +577,7 @@ void tb_learn_free(tb_ctx* c) {
     for (void* p : {(void*)L->w, (void*)L->gw, (void*)L->m, (void*)L->v, (void*)L->P0, (void*)L->P1, (void*)L->samples,
                     (void*)L->meta, (void*)L->wmode,
                     (void*)L->d_pos, (void*)L->s.X, (void*)L->s.out, (void*)L->s.scl, (void*)L->s.jmax, (void*)L->s.invD,
-                    (void*)L->s.mfeat, (void*)L->s.g0, (void*)L->s.tally})
+                    (void*)L->s.mfeat, (void*)L->s.g0, (void*)L->s.tally, (void*)L->s.gate})
         if (p) cudaFree(p);
     delete L;
     c->learn = nullptr;
@@ -627,12 +627,15 @@ int tb_learn_enable(tb_ctx* c, int on) {
     if (r) return r;
     if (!c->cfg.warm_start) { tb_set_error("the learned correction needs a warm start (warm_start > 0)"); return TB_ERR_STATE; }
     Learn* L = get(c);
+    if (on < 0 || on > 2) { tb_set_error("tb_learn_enable: mode must be 0, 1 or 2"); return TB_ERR_ARG; }
     if (on) {
         const size_t hid = (size_t)2 * c->g.K * LC * c->g.nx * c->g.ny;
         if ((r = dalloc(&L->P0, hid)) || (r = dalloc(&L->P1, hid))) return r;
+        if ((r = dalloc(&L->s.gate, 17))) return r;
     }
     TB_CUDA(cudaStreamSynchronize(c->stream));
     L->s.infer = on != 0;
+    L->s.gated = (on == 2) ? 1 : 0;
     tb_graph_reset(c);
     return TB_OK;
 }
@@ -812,6 +815,11 @@ int tb_learn_get_stats(tb_ctx* c, tb_learn_stats* st) {
     TB_CUDA(cudaStreamSynchronize(c->stream));
     TB_CUDA(cudaMemcpy(t.data(), L->s.tally, t.size() * sizeof(long long), cudaMemcpyDeviceToHost));
     for (int k = 0; k < K; k++) { st->tried += t[2 * k]; st->kept += t[2 * k + 1]; }
+    if (L->s.gate) {
+        int g[16];
+        TB_CUDA(cudaMemcpy(g, L->s.gate, sizeof g, cudaMemcpyDeviceToHost));
+        for (int s = 0; s < 4; s++) { st->evaluated += g[4 * s + 2]; st->solves += g[4 * s + 3]; }
+    }
     st->samples = L->count;
     st->capacity = L->cap;
     st->loss = L->last_loss;

@@ -586,10 +586,25 @@ __global__ void k_learn_judge(MgDev M, unsigned* jmax, const int* valid, int nx)
     if ((threadIdx.x & 31) == 0) atomicMax(&jmax[k], __float_as_uint(m));
 }
 
+// Gated evaluation of the network for one stage's solve: evaluate when the
+// last evaluation kept a correction for some mode, when `probe` solves have
+// passed since it, and the first time; else fall back to the guess without
+// running the network.  g: [since last evaluation, kept at it, evaluations,
+// solves].  The decision goes to a conditional graph node (h) or, for
+// host-launched solves, to *flag.
+__global__ void k_learn_gate(int* g, int probe, cudaGraphConditionalHandle h, int use_handle, int* flag) {
+    const int run = (g[2] == 0 || g[1] > 0 || g[0] >= probe - 1) ? 1 : 0;
+    if (run) { g[0] = 0; g[1] = 0; g[2] += 1; }
+    else g[0] += 1;
+    g[3] += 1;
+    if (use_handle) cudaGraphSetConditional(h, (unsigned)run);
+    else *flag = run;
+}
+
 // Keep the candidate for a mode when it lowers the max defect; count the
 // solves tried and the corrections kept; clear the maxima for the loop.
 __global__ void k_learn_keep(unsigned long long* maxsq, unsigned* jmax, int* keep, long long* tally, const int* valid,
-                             int K) {
+                             int K, int* gate_kept) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
     int ok = 0;
@@ -599,6 +614,7 @@ __global__ void k_learn_keep(unsigned long long* maxsq, unsigned* jmax, int* kee
         ok = d1 < d0;
         tally[2 * k] += 1;
         tally[2 * k + 1] += ok;
+        if (ok && gate_kept) atomicAdd(gate_kept, 1);
     }
     keep[2 * k] = ok;
     keep[2 * k + 1] = 0;
@@ -1136,22 +1152,77 @@ static int learned_first(tb_ctx* c, const MgDev& M, int ws, LearnSolve* L) {
         TB_CUDA(cudaMemsetAsync(m->maxsq, 0, K * sizeof(unsigned long long), c->stream));
         return TB_OK;
     }
-    if ((r = tb_learn_run_net(c))) return r;
-    const size_t per = (size_t)(nx - 2) * (ny - 1);
-    k_learn_emit<<<tb_blocks(per * K, 256), 256, 0, c->stream>>>(M, L->out, L->scl, valid, nx);
+    int* gk = L->gated ? L->gate + 4 * ws + 1 : nullptr;
+    // the network, its judge and the kept corrections; when it does not run,
+    // maxsq keeps the guess's defect, which the loop's first defect recomputes
+    auto network = [&]() -> int {
+        int rr;
+        if ((rr = tb_learn_run_net(c))) return rr;
+        const size_t per = (size_t)(nx - 2) * (ny - 1);
+        k_learn_emit<<<tb_blocks(per * K, 256), 256, 0, c->stream>>>(M, L->out, L->scl, valid, nx);
+        TB_CHECK_LAUNCH(c);
+        k_resid<<<tb_blocks(per * K, 256), 256, 0, c->stream>>>(M, 0);
+        TB_CHECK_LAUNCH(c);
+        const unsigned nj = std::min<unsigned>(tb_blocks(per, 256), 64);
+        k_learn_judge<<<dim3(nj, K), 256, 0, c->stream>>>(M, L->jmax, valid, nx);
+        TB_CHECK_LAUNCH(c);
+        k_learn_keep<<<tb_blocks(K, 64), 64, 0, c->stream>>>(m->maxsq, L->jmax, m->lkeep, L->tally, valid, K, gk);
+        TB_CHECK_LAUNCH(c);
+        MgDev Mk = M;
+        Mk.state = m->lkeep;
+        dim3 tgrid(tb_blocks(nx, 32), tb_blocks(ny, 32), K), tblk(32, 8);
+        k_apply<<<tgrid, tblk, 0, c->stream>>>(Mk, c->pfc, c->g.lvl_elems, nx, ny);
+        TB_CHECK_LAUNCH(c);
+        return TB_OK;
+    };
+    if (!L->gated) return network();
+    if (!c->capturing) {
+        k_learn_gate<<<1, 1, 0, c->stream>>>(L->gate + 4 * ws, L->probe, 0, 0, L->gate + 16);
+        TB_CHECK_LAUNCH(c);
+        int run = 0;
+        TB_CUDA(cudaMemcpyAsync(&run, L->gate + 16, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        TB_CUDA(cudaStreamSynchronize(c->stream));
+        return run ? network() : TB_OK;
+    }
+    // recorded step: the network's kernels become the body of a conditional
+    // IF node whose condition the gate kernel sets at every replay
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    TB_CUDA(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, nullptr, nullptr, nullptr));
+    if (st != cudaStreamCaptureStatusActive || !g) { tb_set_error("step graph: stream is not recording"); return TB_ERR_STATE; }
+    cudaGraphConditionalHandle h;
+    TB_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+    k_learn_gate<<<1, 1, 0, c->stream>>>(L->gate + 4 * ws, L->probe, h, 1, nullptr);
     TB_CHECK_LAUNCH(c);
-    k_resid<<<tb_blocks(per * K, 256), 256, 0, c->stream>>>(M, 0);
-    TB_CHECK_LAUNCH(c);
-    const unsigned nj = std::min<unsigned>(tb_blocks(per, 256), 64);
-    k_learn_judge<<<dim3(nj, K), 256, 0, c->stream>>>(M, L->jmax, valid, nx);
-    TB_CHECK_LAUNCH(c);
-    k_learn_keep<<<tb_blocks(K, 64), 64, 0, c->stream>>>(m->maxsq, L->jmax, m->lkeep, L->tally, valid, K);
-    TB_CHECK_LAUNCH(c);
-    MgDev Mk = M;
-    Mk.state = m->lkeep;
-    dim3 tgrid(tb_blocks(nx, 32), tb_blocks(ny, 32), K), tblk(32, 8);
-    k_apply<<<tgrid, tblk, 0, c->stream>>>(Mk, c->pfc, c->g.lvl_elems, nx, ny);
-    TB_CHECK_LAUNCH(c);
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    TB_CUDA(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphNodeParams p = {};
+    std::memset(&p, 0, sizeof p);
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    TB_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+    TB_CUDA(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    cudaStream_t outer = c->stream;
+    c->stream = c->body_stream;
+    cudaError_t e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) {
+        c->stream = outer;
+        tb_set_error("step graph: recording the learned correction: %s", cudaGetErrorString(e));
+        return TB_ERR_CUDA;
+    }
+    const long long l0 = c->launches;
+    r = network();
+    if (c->g_stage >= 1 && c->g_stage <= 4) c->g_learn[c->g_stage - 1] = c->launches - l0;
+    cudaGraph_t got = nullptr;
+    e = cudaStreamEndCapture(c->stream, &got);
+    c->stream = outer;
+    if (r) return r;
+    if (e != cudaSuccess) { tb_set_error("step graph: recording the learned correction: %s", cudaGetErrorString(e)); return TB_ERR_CUDA; }
     return TB_OK;
 }
 
