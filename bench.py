@@ -48,6 +48,9 @@ def parse():
     p.add_argument("--workload", default="config2", choices=["config2", "config5", "medium", "small"],
                    help="config5: 2049x257x64 with LES and a roughness element; medium: 513x193x16, small: "
                         "129x65x8 grids for profiler captures")
+    p.add_argument("--no-learned", action="store_true",
+                   help="mixed form without the learned first correction (by default it runs gated, with the "
+                        "weights of trans_bl_gb300/data/learned_config4.f32 when the workload is config 2)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
@@ -352,6 +355,14 @@ def main():
     # launch shapes timed on this grid (scratch fields only)
     tune = ({"xline_warps": 0, "yline_threads": 0, "nl_blocks_per_sm": 0} if args.no_autotune else ctx.autotune())
     pts = cfg.nx * cfg.ny * cfg.kfour
+    # the learned first correction (config 4's network, trained on this grid
+    # by trans_bl_gb300/learn_config4.py), gated: it runs in the solve after
+    # one where it helped and once every 16 solves of a stage
+    wpath = os.path.join(ROOT, "trans_bl_gb300", "data", "learned_config4.f32")
+    learned = (form == "mixed" and not args.no_learned and WORKLOAD["name"] == "config2" and os.path.exists(wpath))
+    if learned:
+        ctx.learn_set_weights(np.fromfile(wpath, dtype=np.float32))
+        ctx.learn_enable(True, gated=True)
     # start from a disturbed state past the one-period forcing ramp, so every
     # mode carries a disturbance and every solve does work
     t0 = cfg.stpp + 1
@@ -365,6 +376,8 @@ def main():
             state2 = ctx.get_state()
     ctx.synchronize()
     launches0 = ctx.launch_count()
+    vc0 = ctx.poisson_stats()["total_vcycles"]
+    ls0 = ctx.learn_stats() if learned else None
     barrier(dist)
     torch.cuda.synchronize()
     with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
@@ -373,6 +386,15 @@ def main():
     torch.cuda.synchronize()
     barrier(dist)
     launches = ctx.launch_count() - launches0
+    vcycles_per_step = (ctx.poisson_stats()["total_vcycles"] - vc0) / args.steps
+    learned_line = None
+    if learned:
+        ls1 = ctx.learn_stats()
+        d = {k: ls1[k] - ls0[k] for k in ("solves", "evaluated", "tried", "kept")}
+        learned_line = dict(d, fallback_rate=1.0 - d["evaluated"] / max(d["solves"], 1),
+                            kept_share=d["kept"] / max(d["tried"], 1),
+                            network="4 conv layers 4-32-32-32-1, 3x3, GELU, FP32 on CUDA cores",
+                            weights="trans_bl_gb300/data/learned_config4.f32")
     # kernel-family breakdown from CUDA events, on further steps outside the
     # timed region (the events themselves cost ~10% of a step)
     ctx.profile(True)
@@ -424,7 +446,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == "plain" else "f64+f32",
             "data": "synthetic (Falkner-Skan base flow, generated coefficients, seeded TS forcing phases, "
                     "seeded smooth disturbance)",
-            "config": {"workload": workload_name(cfg), "form": form, "replicas": world,
+            "config": {"workload": workload_name(cfg),
+                       "form": (form + "+learned (gated)") if learned else form, "replicas": world,
                        "step": "replayed CUDA graph" if (cfg.step_graph and form == "mixed") else "host-launched kernels",
                        "l2": "inputs larger than L2: working set ~5 GB vs 129 MB L2",
                        "start": "disturbed state (1e-3) past the forcing ramp",
@@ -432,7 +455,8 @@ def main():
                                                               "plain_line_warps_multi", "plain_line_warps_single")
                                          if k in tune},
                        "iterations_per_mode_last_solve": float(np.mean(stats["vcycles"][:cfg.kfour]))},
-            "roofline": roof, "gpu_launches": launches,
+            "roofline": roof, "gpu_launches": launches, "vcycles_per_step": vcycles_per_step,
+            "learned": learned_line,
             "breakdown_ms": dict({f: v[0] for f, v in fam.items()}, profiled_steps=prof_steps, profiled_total=prof_ms),
             "clocks": clk.summary()}
     if not args.no_e2e:
