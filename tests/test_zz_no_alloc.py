@@ -69,6 +69,7 @@ def test_noalloc_filter_by_slices_of_modes():
     pp = [parts.device_field(w) for w in (3, 4, 5)]
     api.check(lib.tb_filter_trid_noalloc(pw[0], pw[1], pw[2], cfg.nx, cfg.ny, cfg.kfour, cfg.alphaf,
                                          whole.stream()), "tb_filter_trid_noalloc")
+    whole.synchronize()   # calls that overlap on the GPU race on the shared scratch array
     k1 = cfg.kfour // 2
     step = cfg.nx * cfg.ny * 16   # bytes per Fourier mode of a complex*16 field
     for k0, nk in ((0, k1), (k1, cfg.kfour - k1)):
