@@ -303,6 +303,25 @@ def plain_comparison(coefs, base, mixed_state2, t0, hbm_peak):
     err = {n: float(np.max(np.abs(mixed_state2[n] - sp[n])) / max(np.max(np.abs(sp[n])), 1e-300)) for n in NAMES}
     amp = disturbance_amplitude_error(mixed_state2, sp, base)
     ctx.close()
+    # the FP64 rerun the errors are measured against: the plain form with its
+    # solves converged far below the runs' tolerance (1e-12, up to 60 V-cycles),
+    # so that the difference of two forms is not the slack both leave at 1e-10
+    rcfg = workload("plain")
+    rcfg.tol_stage = rcfg.tol_final = 1e-12
+    rcfg.max_vcycles = 60
+    rctx = api.Context(rcfg, coefs, base)
+    rctx.put_state(start_state(rcfg, base))
+    for q in range(2):
+        rctx.step(t0 + q)
+    sr = rctx.get_state()
+    rres = rctx.poisson_stats()["residual"][:rcfg.kfour]
+    rctx.close()
+    def against(st):
+        return {"fields": {n: float(np.max(np.abs(st[n] - sr[n])) / max(np.max(np.abs(sr[n])), 1e-300)) for n in NAMES},
+                "disturbance_amplitude": disturbance_amplitude_error(st, sr, base)}
+    rerun = {"what": "plain FP64 form, Poisson tolerance 1e-12 (up to 60 V-cycles), 2 steps from the same state",
+             "max_poisson_residual": float(np.max(rres)),
+             "mixed": against(mixed_state2), "plain_at_1e-10": against(sp)}
     pts = cfg.nx * cfg.ny * cfg.kfour
     ms = min(ms1, ms2)
     nv = float(0.5 * (nv1 + nv2))
@@ -316,7 +335,8 @@ def plain_comparison(coefs, base, mixed_state2, t0, hbm_peak):
                               "frac": value * 1e6 * B / 1e9 / hbm_peak},
             "mixed_vs_plain_rel_err_after_2_steps": err,
             "max_rel_err": max(err.values()),
-            "disturbance_amplitude_rel_err": amp}
+            "disturbance_amplitude_rel_err": amp,
+            "fp64_rerun": rerun}
 
 
 def disturbance_amplitude_error(a, b, base):
@@ -467,6 +487,9 @@ def main():
     if rank == 0 and world == 1 and form == "mixed" and not args.no_plain and state2 is not None:
         line["plain_fp64"] = plain_comparison(coefs, base, state2, t0, hbm_peak)
         line["speedup_vs_plain"] = value / line["plain_fp64"]["value"]
+        # the metric's error bound: TS-disturbance amplitude of the timed form
+        # against the converged FP64 rerun, after two steps from the same state
+        line["ts_amp_rel_err"] = line["plain_fp64"]["fp64_rerun"]["mixed"]["disturbance_amplitude"]["max"]
     if rank == 0 and world == 1 and form == "mixed" and not args.no_ensemble:
         line["ensemble"] = ensemble_measure(max(1, min(args.steps, 5)), 3)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
