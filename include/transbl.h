@@ -202,7 +202,7 @@ int tb_dft_matrix(int P, int forward, double* out);
    A convolutional network (four 3x3 layers, 4 -> 32 -> 32 -> 32 -> 1
    channels, GELU) estimates, per mode, the error of the extrapolated guess
    from v(t-1), v(t-1) - v(t-2) and the FP64 defect of the guess.  Its
-   correction is kept per mode only where it lowers the max defect; the
+   correction is kept per mode only where it lowers the max defect by 5%; the
    multigrid then iterates to the same tolerance.  The solver generates the
    training crops itself, and the network is trained on the GPU by the
    library's own forward and backward kernels (Adam).  Needs the mixed form

@@ -197,11 +197,11 @@ def test_learned_graph_matches_host_launched(trained, gated):
         for f in NAMES:
             assert np.array_equal(a[f], b[f]), f
     assert g.learn_stats()["kept"] == e.learn_stats()["kept"]
-    g.close()
-    e.close()
     if gated:
         assert g.learn_stats()["evaluated"] == e.learn_stats()["evaluated"]
         assert g.learn_stats()["solves"] == e.learn_stats()["solves"] == 4 * 6
+    g.close()
+    e.close()
 
 
 @pytest.mark.parametrize("graph", [1, 0])

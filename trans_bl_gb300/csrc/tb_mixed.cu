@@ -601,7 +601,9 @@ __global__ void k_learn_gate(int* g, int probe, cudaGraphConditionalHandle h, in
     else *flag = run;
 }
 
-// Keep the candidate for a mode when it lowers the max defect; count the
+// Keep the candidate for a mode when it lowers the max defect by 5% or more
+// (max|d0 - L e|^2 < 0.9 max|d0|^2: a zero correction, whose FP32 defect
+// differs from the FP64 one by rounding only, is never kept); count the
 // solves tried and the corrections kept; clear the maxima for the loop.
 __global__ void k_learn_keep(unsigned long long* maxsq, unsigned* jmax, int* keep, long long* tally, const int* valid,
                              int K, int* gate_kept) {
@@ -611,7 +613,7 @@ __global__ void k_learn_keep(unsigned long long* maxsq, unsigned* jmax, int* kee
     if (*valid >= 2) {
         const double d0 = __longlong_as_double((long long)maxsq[k]);
         const double d1 = (double)__uint_as_float(jmax[k]);
-        ok = d1 < d0;
+        ok = d1 < 0.9 * d0;
         tally[2 * k] += 1;
         tally[2 * k + 1] += ok;
         if (ok && gate_kept) atomicAdd(gate_kept, 1);

@@ -67,9 +67,29 @@ def main():
     p.add_argument("--crops", type=int, default=20000)
     p.add_argument("--iters", type=int, default=4000)
     p.add_argument("--eval-steps", type=int, default=16)
+    p.add_argument("--weights", default=None,
+                   help="evaluate these weights (float32 file) instead of training; writes learned_config4_eval.json")
     a = p.parse_args()
     cfg = configs.config2(tol=1e-10, precision=api.FORM_MIXED)
     coefs, base = configs.setup_inputs(cfg)
+    if a.weights:
+        w = np.fromfile(a.weights, dtype=np.float32)
+        g = api.Context(cfg, coefs, base)
+        g.put_state(configs.disturbed_state(cfg, base, np.random.default_rng(41)))
+        t = cfg.stpp + 1
+        for q in range(8):
+            g.step(t + q)
+        state = g.get_state()
+        g.close()
+        res = {"weights": os.path.basename(a.weights), "F_1e-4": compare(cfg, coefs, base, state, t + 10, w, a.eval_steps)}
+        cfg2 = configs.config2(tol=1e-10, precision=api.FORM_MIXED, F=1.2e-4)
+        coefs2, base2 = configs.setup_inputs(cfg2)
+        st2 = configs.disturbed_state(cfg2, base2, np.random.default_rng(42))
+        res["F_1.2e-4"] = compare(cfg2, coefs2, base2, st2, cfg2.stpp + 3, w, a.eval_steps)
+        os.makedirs(a.out, exist_ok=True)
+        json.dump(res, open(os.path.join(a.out, "learned_config4_eval.json"), "w"), indent=1)
+        print(json.dumps(res))
+        return
     g = api.Context(cfg, coefs, base)
     g.put_state(configs.disturbed_state(cfg, base, np.random.default_rng(41)))
     t = cfg.stpp + 1
