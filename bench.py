@@ -376,8 +376,8 @@ def main():
     tune = ({"xline_warps": 0, "yline_threads": 0, "nl_blocks_per_sm": 0} if args.no_autotune else ctx.autotune())
     pts = cfg.nx * cfg.ny * cfg.kfour
     # the learned first correction (config 4's network, trained on this grid
-    # by trans_bl_gb300/learn_config4.py), gated: it runs in the solve after
-    # one where it helped and once every 16 solves of a stage
+    # by trans_bl_gb300/learn_config4.py), gated: it runs once every 32 solves
+    # of a stage and stays on while a solve with it needs fewer corrections
     wpath = os.path.join(ROOT, "trans_bl_gb300", "data", "learned_config4.f32")
     learned = (form == "mixed" and not args.no_learned and WORKLOAD["name"] == "config2" and os.path.exists(wpath))
     if learned:

@@ -223,9 +223,10 @@ int tb_learn_init(tb_ctx* ctx, unsigned long long seed);   /* He-normal, last la
 int tb_learn_set_weights(tb_ctx* ctx, const float* w);
 int tb_learn_get_weights(tb_ctx* ctx, float* w);
 /* on = 1: run the network in every solve; on = 2 (gated): a stage runs it
-   in the solve after one where it kept a correction for some mode, and
-   otherwise once every 16 solves, falling back to the guess without running
-   it in between; 0: off.                                                   */
+   in its first solve and once every 32 solves, and keeps running it while a
+   solve with it needs fewer multigrid corrections than the stage's last
+   solve without it; in between the solve falls back to the guess without
+   running the network; 0: off.                                             */
 int tb_learn_enable(tb_ctx* ctx, int on);
 /* Collect crops_per_solve crops from every solve into a buffer of `capacity`
    crops; capacity 0 stops collecting and keeps the crops for training.     */

@@ -207,7 +207,7 @@ def test_learned_graph_matches_host_launched(trained, gated):
 @pytest.mark.parametrize("graph", [1, 0])
 def test_gated_falls_back(trained, graph):
     """A network that never helps (zero output: the last layer starts at
-    zero) runs only in a stage's first solve and then once every 16 solves;
+    zero) runs only in a stage's first solve and then once every 32 solves;
     the fields are those of the form without it, bit for bit."""
     from trans_bl_gb300 import api
     cfg0, coefs, base, state, t, w, _, _ = trained
@@ -219,13 +219,13 @@ def test_gated_falls_back(trained, graph):
     g.learn_enable(True, gated=True)
     for c in (g, ref):
         c.put_state(state)
-    n = 20
+    n = 36
     for q in range(n):
         g.step(t + q)
         ref.step(t + q)
     st = g.learn_stats()
     assert st["solves"] == 4 * n
-    assert st["evaluated"] == 4 * 2          # solves 1 and 17 of each stage
+    assert st["evaluated"] == 4 * 2          # solves 1 and 33 of each stage
     assert st["kept"] == 0
     a, b = g.get_state(), ref.get_state()
     for f in NAMES:

@@ -381,8 +381,8 @@ class Context:
         self._c(self.lib.tb_learn_set_weights(self.h, fptr(w)), "tb_learn_set_weights")
 
     def learn_enable(self, on=True, gated=False):
-        """Apply the learned correction in every solve (on), or gated: only in
-        the solve after one where it helped and once every 16 solves (gated)."""
+        """Apply the learned correction in every solve (on), or gated: once
+        every 32 solves of a stage, and on while it saves corrections (gated)."""
         mode = (2 if gated else 1) if on else 0
         self._c(self.lib.tb_learn_enable(self.h, mode), "tb_learn_enable")
 

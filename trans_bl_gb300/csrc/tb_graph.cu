@@ -111,11 +111,11 @@ int read_back(tb_ctx* c, const int* hs, const double* he) {
     // the learned correction's kernels ran in the replays whose gate opened
     LearnSolve* L = tb_learn_solve(c);
     if (L && L->gated && L->gate) {
-        int g[16];
+        int g[32];
         if (cudaMemcpy(g, L->gate, sizeof g, cudaMemcpyDeviceToHost) == cudaSuccess)
             for (int s = 0; s < 4; s++) {
-                n += c->g_learn[s] * (g[4 * s + 2] - c->g_learn_seen[s]);
-                c->g_learn_seen[s] = g[4 * s + 2];
+                n += c->g_learn[s] * (g[8 * s + 2] - c->g_learn_seen[s]);
+                c->g_learn_seen[s] = g[8 * s + 2];
             }
     }
     c->launches += n;

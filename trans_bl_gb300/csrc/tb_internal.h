@@ -230,11 +230,12 @@ struct LearnSolve {
     float* mfeat = nullptr;      // (K, ny) share of k^2 beta^2 in the diagonal
     cplx* g0 = nullptr;          // guess before any correction (while sampling)
     long long* tally = nullptr;  // (K, 2) solves tried / corrections kept per mode
-    // gated evaluation (tb_learn_enable mode 2): per stage [since last
-    // evaluation, modes kept at it, evaluations, solves]
+    // gated evaluation (tb_learn_enable mode 2): per stage [solves since it
+    // last ran, ran in the last solve, evaluations, solves, corrections of
+    // the last solve without / with it, 2 spare]
     int gated = 0;
-    int probe = 16;              // a stage evaluates the network at least every `probe` solves
-    int* gate = nullptr;         // (4, 4)
+    int probe = 32;              // a stage evaluates the network at least every `probe` solves
+    int* gate = nullptr;         // (4, 8) and a host-read flag
 };
 // The fine-level FP32 operator of the mixed form (the operator of k_resid at
 // level 0): device tables and scalars.

@@ -631,7 +631,7 @@ int tb_learn_enable(tb_ctx* c, int on) {
     if (on) {
         const size_t hid = (size_t)2 * c->g.K * LC * c->g.nx * c->g.ny;
         if ((r = dalloc(&L->P0, hid)) || (r = dalloc(&L->P1, hid))) return r;
-        if ((r = dalloc(&L->s.gate, 17))) return r;
+        if ((r = dalloc(&L->s.gate, 33))) return r;
     }
     TB_CUDA(cudaStreamSynchronize(c->stream));
     L->s.infer = on != 0;
@@ -816,9 +816,9 @@ int tb_learn_get_stats(tb_ctx* c, tb_learn_stats* st) {
     TB_CUDA(cudaMemcpy(t.data(), L->s.tally, t.size() * sizeof(long long), cudaMemcpyDeviceToHost));
     for (int k = 0; k < K; k++) { st->tried += t[2 * k]; st->kept += t[2 * k + 1]; }
     if (L->s.gate) {
-        int g[16];
+        int g[32];
         TB_CUDA(cudaMemcpy(g, L->s.gate, sizeof g, cudaMemcpyDeviceToHost));
-        for (int s = 0; s < 4; s++) { st->evaluated += g[4 * s + 2]; st->solves += g[4 * s + 3]; }
+        for (int s = 0; s < 4; s++) { st->evaluated += g[8 * s + 2]; st->solves += g[8 * s + 3]; }
     }
     st->samples = L->count;
     st->capacity = L->cap;

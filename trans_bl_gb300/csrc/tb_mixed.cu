@@ -586,19 +586,37 @@ __global__ void k_learn_judge(MgDev M, unsigned* jmax, const int* valid, int nx)
     if ((threadIdx.x & 31) == 0) atomicMax(&jmax[k], __float_as_uint(m));
 }
 
-// Gated evaluation of the network for one stage's solve: evaluate when the
-// last evaluation kept a correction for some mode, when `probe` solves have
-// passed since it, and the first time; else fall back to the guess without
-// running the network.  g: [since last evaluation, kept at it, evaluations,
-// solves].  The decision goes to a conditional graph node (h) or, for
-// host-launched solves, to *flag.
+// Gated evaluation of the network for one stage's solve.  It runs the first
+// time, once every `probe` solves, and in the solve after one where it ran
+// and the solve needed fewer corrections than the stage's last solve
+// without it: the network is kept on only while it saves multigrid work;
+// otherwise the solve falls back to the warm-start guess without running it.
+// g (per stage): [solves since it last ran, ran in the last solve,
+// evaluations, solves, corrections of the last solve without it, of the
+// last solve with it].  The decision goes to a conditional graph node (h)
+// or, for host-launched solves, to *flag.
 __global__ void k_learn_gate(int* g, int probe, cudaGraphConditionalHandle h, int use_handle, int* flag) {
-    const int run = (g[2] == 0 || g[1] > 0 || g[0] >= probe - 1) ? 1 : 0;
-    if (run) { g[0] = 0; g[1] = 0; g[2] += 1; }
+    const int saved = g[1] && g[5] < g[4];
+    const int run = (g[2] == 0 || saved || g[0] >= probe - 1) ? 1 : 0;
+    if (run) { g[0] = 0; g[2] += 1; }
     else g[0] += 1;
+    g[1] = run;
     g[3] += 1;
     if (use_handle) cudaGraphSetConditional(h, (unsigned)run);
     else *flag = run;
+}
+
+// After a gated solve: its corrections (the largest count over the modes)
+// into the stage's slot for solves with or without the network.
+__global__ void k_learn_after(const int* state, int K, int* g) {
+    int c = 0;
+    for (int k = 0; k < K; k++) {
+        int v = state[2 * k + 1];
+        if (v < 0) v = -v - 1;
+        c = max(c, v);
+    }
+    if (g[1]) g[5] = c;
+    else g[4] = c;
 }
 
 // Keep the candidate for a mode when it lowers the max defect by 5% or more
@@ -1154,7 +1172,7 @@ static int learned_first(tb_ctx* c, const MgDev& M, int ws, LearnSolve* L) {
         TB_CUDA(cudaMemsetAsync(m->maxsq, 0, K * sizeof(unsigned long long), c->stream));
         return TB_OK;
     }
-    int* gk = L->gated ? L->gate + 4 * ws + 1 : nullptr;
+    int* gk = nullptr;
     // the network, its judge and the kept corrections; when it does not run,
     // maxsq keeps the guess's defect, which the loop's first defect recomputes
     auto network = [&]() -> int {
@@ -1179,10 +1197,10 @@ static int learned_first(tb_ctx* c, const MgDev& M, int ws, LearnSolve* L) {
     };
     if (!L->gated) return network();
     if (!c->capturing) {
-        k_learn_gate<<<1, 1, 0, c->stream>>>(L->gate + 4 * ws, L->probe, 0, 0, L->gate + 16);
+        k_learn_gate<<<1, 1, 0, c->stream>>>(L->gate + 8 * ws, L->probe, 0, 0, L->gate + 32);
         TB_CHECK_LAUNCH(c);
         int run = 0;
-        TB_CUDA(cudaMemcpyAsync(&run, L->gate + 16, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        TB_CUDA(cudaMemcpyAsync(&run, L->gate + 32, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         TB_CUDA(cudaStreamSynchronize(c->stream));
         return run ? network() : TB_OK;
     }
@@ -1194,7 +1212,7 @@ static int learned_first(tb_ctx* c, const MgDev& M, int ws, LearnSolve* L) {
     if (st != cudaStreamCaptureStatusActive || !g) { tb_set_error("step graph: stream is not recording"); return TB_ERR_STATE; }
     cudaGraphConditionalHandle h;
     TB_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
-    k_learn_gate<<<1, 1, 0, c->stream>>>(L->gate + 4 * ws, L->probe, h, 1, nullptr);
+    k_learn_gate<<<1, 1, 0, c->stream>>>(L->gate + 8 * ws, L->probe, h, 1, nullptr);
     TB_CHECK_LAUNCH(c);
     const cudaGraphNode_t* deps = nullptr;
     size_t nd = 0;
@@ -1347,6 +1365,10 @@ int tb_poi_uy_mixed(tb_ctx* c, const cplx* dwzdx, double erro) {
             k_apply<<<tgrid, tblk, 0, c->stream>>>(M, c->pfc, c->g.lvl_elems, nx, ny);
             TB_CHECK_LAUNCH(c);
         }
+    }
+    if (L && L->infer && L->gated) {
+        k_learn_after<<<1, 1, 0, c->stream>>>(c->pstate, K, L->gate + 8 * ws);
+        TB_CHECK_LAUNCH(c);
     }
     if (L && L->sample && !c->capturing && hv >= 2 && (r = tb_learn_collect(c))) return r;
     if ((r = tb_poisson_end(c))) return r;
