@@ -158,6 +158,7 @@ def workload(form, make_default=None):
     if WORKLOAD["name"] == "medium":
         return configs.blasius_ts_config(513, 193, 16, 32, 4, steps_per_period=1024, amp2d=1e-4, amp3d=1e-5, **kw)
     if WORKLOAD["name"] == "config5":
+        kw["tol"] = 1e-8
         return configs.config5(**kw)
     return configs.config2(**kw)
 
@@ -172,10 +173,10 @@ def product_library_mapped():
 
 
 def workload_name(cfg):
-    name = "blasius_ts_3d nx=%d ny=%d kfour=%d kphys=%d msh=%d tol=1e-10 steps_per_period=%d" % (
-        cfg.nx, cfg.ny, cfg.kfour, cfg.kphys, cfg.msh, cfg.stpp)
+    name = "blasius_ts_3d nx=%d ny=%d kfour=%d kphys=%d msh=%d tol=%g steps_per_period=%d" % (
+        cfg.nx, cfg.ny, cfg.kfour, cfg.kphys, cfg.msh, cfg.tol_stage, cfg.stpp)
     if cfg.my_form == 4:
-        name += " les C_s=%g A+=%g" % (cfg.C_s, cfg.A_plus)
+        name += " les C_s=%g A+=%g damping=%d" % (cfg.C_s, cfg.A_plus, cfg.les_damping)
     if cfg.ibm:
         name += " roughness h=%.3g R=%.3g at x=%.3g irf=%.4g" % (cfg.ibm_h, cfg.ibm_R, cfg.ibm_xc, cfg.irf)
     return name
@@ -305,9 +306,12 @@ def plain_comparison(coefs, base, mixed_state2, t0, hbm_peak):
     ctx.close()
     # the FP64 rerun the errors are measured against: the plain form with its
     # solves converged far below the runs' tolerance (1e-12, up to 60 V-cycles),
-    # so that the difference of two forms is not the slack both leave at 1e-10
+    # so that the difference of two forms is not the slack both leave at 1e-10;
+    # on the 2049x257 grid the FP64 defect's round-off (~6e-9) leaves no room
+    # below the run's own 1e-8
     rcfg = workload("plain")
-    rcfg.tol_stage = rcfg.tol_final = 1e-12
+    rtol = rcfg.tol_stage if WORKLOAD["name"] == "config5" else 1e-12
+    rcfg.tol_stage = rcfg.tol_final = rtol
     rcfg.max_vcycles = 60
     rctx = api.Context(rcfg, coefs, base)
     rctx.put_state(start_state(rcfg, base))
@@ -319,9 +323,9 @@ def plain_comparison(coefs, base, mixed_state2, t0, hbm_peak):
     def against(st):
         return {"fields": {n: float(np.max(np.abs(st[n] - sr[n])) / max(np.max(np.abs(sr[n])), 1e-300)) for n in NAMES},
                 "disturbance_amplitude": disturbance_amplitude_error(st, sr, base)}
-    rerun = {"what": "plain FP64 form, Poisson tolerance 1e-12 (up to 60 V-cycles), 2 steps from the same state",
+    rerun = {"what": "plain FP64 form, Poisson tolerance %g (up to 60 V-cycles), 2 steps from the same state" % rtol,
              "max_poisson_residual": float(np.max(rres)),
-             "mixed": against(mixed_state2), "plain_at_1e-10": against(sp)}
+             "mixed": against(mixed_state2), "plain_at_run_tolerance": against(sp)}
     pts = cfg.nx * cfg.ny * cfg.kfour
     ms = min(ms1, ms2)
     nv = float(0.5 * (nv1 + nv2))

@@ -60,7 +60,9 @@ typedef struct tb_config {
     int    max_vcycles; /* V-cycle cap (11 in the reference)  poisson_par.f:33      */
     int    ibm;         /* 1: add immersed-boundary force (cvirt)                   */
     int    precision;   /* TB_FORM_PLAIN_FP64 or TB_FORM_MIXED                      */
-    int    les_damping; /* 0: reference cubic damping, 1: van Driest [1-e^{-y+/A}]^2*/
+    int    les_damping; /* 0: reference cubic damping 1-e^{-(y+/A)^3}, 1: van Driest
+                           [1-e^{-y+/A}]^2; +2: y+ from |wall vorticity| (les_par.f:194
+                           takes sqrt(Re wz_wall), undefined where wz_wall < 0)      */
     int    warm_start;  /* mixed form: 1 starts each stage's v-Poisson solve from the
                            extrapolation 2 v(t-1) - v(t-2) of the same stage's solutions
                            of the two previous steps; 2 from the current v plus the

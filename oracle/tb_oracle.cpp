@@ -1089,9 +1089,13 @@ void les_terms_impl(ora_ctx* o, C* Fx, C* Fy, C* Fz) {
             double y = (o->stf == 1.0) ? (double)(j - 1) * o->dy : o->dy * (powi(o->stf, j - 1) - 1.0) / (o->stf - 1.0);
             for (int i = 1; i <= o->nx; i++) {
                 size_t q = o->id2(i, j) + n2 * (z - 1);
-                double yplus = std::sqrt(o->Re * o->wz[o->id(i, 1, 1)].re / std::sqrt(o->fac_y)) * y;
+                // les_par.f:194; les_damping bit 2 takes |wz_wall| (the reference's
+                // square root is NaN where the wall vorticity is negative)
+                double wz0 = o->wz[o->id(i, 1, 1)].re;
+                if (o->cfg.les_damping & 2) wz0 = std::fabs(wz0);
+                double yplus = std::sqrt(o->Re * wz0 / std::sqrt(o->fac_y)) * y;
                 double damp;
-                if (o->cfg.les_damping == 1) {
+                if (o->cfg.les_damping & 1) {
                     double e = 1.0 - std::exp(-yplus / o->cfg.A_plus);
                     damp = e * e;
                 } else {

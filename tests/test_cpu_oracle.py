@@ -75,3 +75,28 @@ def test_stage_runs_finite(case):
     for n, f in s.items():
         assert np.all(np.isfinite(f)), n
     assert np.max(np.abs(s["uy"][0, 0])) > 0  # the wall forcing is on
+
+
+@pytest.mark.parametrize("damping", [0, 1])
+def test_les_damping_reversed_wall_shear(lib_built, oracle_built, damping):
+    """les_par.f:194 takes y+ = sqrt(Re wz_wall) y: NaN at stations with a
+    negative mean wall vorticity; with y+ from |wz_wall| (damping + 2) the
+    terms are finite and equal the reference's where wz_wall > 0."""
+    cfg, coefs, base = small_case(my_form=4)
+    cfg.C_s, cfg.A_plus = 0.1, 26.0
+    st = perturbed_state(cfg, base, np.random.default_rng(36))
+    band = slice(cfg.nx // 3, cfg.nx // 3 + 6)
+    out = {}
+    for d in (damping, damping + 2):
+        cfg.les_damping = d
+        o = oracle_built.Oracle(cfg, coefs, base)
+        o.put_state(st)
+        out[d, "pos"] = o.les_terms()
+        s2 = {n: f.copy() for n, f in st.items()}
+        s2["wz"][0, 0, band] = -np.abs(s2["wz"][0, 0, band])
+        o.put_state(s2)
+        out[d, "neg"] = o.les_terms()
+    for a, b in zip(out[damping, "pos"], out[damping + 2, "pos"]):
+        assert np.array_equal(a, b)
+    assert not all(np.all(np.isfinite(a)) for a in out[damping, "neg"])
+    assert all(np.all(np.isfinite(a)) for a in out[damping + 2, "neg"])

@@ -49,12 +49,35 @@ def pair(oracle_built, case, seed):
     return g, o
 
 
-@pytest.mark.parametrize("damping", [0, 1])
+@pytest.mark.parametrize("damping", [0, 1, 2, 3])
 def test_les_terms(oracle_built, damping):
     g, o = pair(oracle_built, les_ibm_case(damping=damping, ibm=0), 31)
     for a, b in zip(g.les_terms(), o.les_terms()):
         assert np.max(np.abs(b)) > 0
         assert rel(a, b) < TOL_TERMS
+
+
+@pytest.mark.parametrize("damping", [2, 3])
+def test_les_terms_reversed_wall_shear(oracle_built, damping):
+    """Mean wall vorticity negative over a band of stations: with y+ taken
+    from |wz_wall| (les_damping 2, 3) both give the same finite terms; the
+    reference's sqrt(Re wz_wall) (damping 0, 1) is NaN there, in both."""
+    from trans_bl_gb300 import api
+    cfg, coefs, base = les_ibm_case(damping=damping, ibm=0)
+    st = perturbed_state(cfg, base, np.random.default_rng(35))
+    band = slice(cfg.nx // 3, cfg.nx // 3 + 6)
+    st["wz"][0, 0, band] = -np.abs(st["wz"][0, 0, band])
+    g = api.Context(cfg, coefs, base)
+    o = oracle_built.Oracle(cfg, coefs, base)
+    g.put_state(st)
+    o.put_state(st)
+    for a, b in zip(g.les_terms(), o.les_terms()):
+        assert np.all(np.isfinite(a)) and np.all(np.isfinite(b))
+        assert rel(a, b) < TOL_TERMS
+    cfg.les_damping = damping - 2
+    g2 = api.Context(cfg, coefs, base)
+    g2.put_state(st)
+    assert not all(np.all(np.isfinite(a)) for a in g2.les_terms())
 
 
 def test_cvirt(oracle_built):
@@ -70,11 +93,11 @@ def test_drv_forced(oracle_built):
         assert rel(a, b) < 1e-11
 
 
-# Form 4 with the roughness element is left out of the step test: the
-# roughness reverses the wall shear within two steps and the damping's
-# y+ = sqrt(Re wz(i,1,1)) y (les_par.f:194) is then NaN, in the reference's
+# Form 4 with the roughness element runs with y+ from |wz_wall| (damping
+# 3): the roughness reverses the wall shear within two steps, where the
+# reference's y+ = sqrt(Re wz(i,1,1)) y (les_par.f:194) is NaN, in its
 # formula as in both implementations.
-@pytest.mark.parametrize("damping,ibm,form", [(0, 0, 4), (1, 0, 4), (0, 1, 0)])
+@pytest.mark.parametrize("damping,ibm,form", [(0, 0, 4), (1, 0, 4), (0, 1, 0), (3, 1, 4)])
 def test_steps_les_ibm(oracle_built, damping, ibm, form):
     case = les_ibm_case(damping=damping, ibm=ibm, my_form=form)
     g, o = pair(oracle_built, case, 34)

@@ -36,6 +36,7 @@ int check_cfg(const tb_config* c) {
     if (c->n_forced < 0 || c->n_forced > 4) { tb_set_error("n_forced must be in [0, 4]"); return TB_ERR_ARG; }
     if (c->precision != TB_FORM_PLAIN_FP64 && c->precision != TB_FORM_MIXED) { tb_set_error("unknown precision form"); return TB_ERR_ARG; }
     if (c->my_form != 0 && c->my_form != 4) { tb_set_error("my_form must be 0 or 4"); return TB_ERR_ARG; }
+    if (c->les_damping < 0 || c->les_damping > 3) { tb_set_error("les_damping must be 0..3"); return TB_ERR_ARG; }
     return TB_OK;
 }
 

@@ -583,9 +583,10 @@ __global__ void __launch_bounds__(128) k_les(LesArgs A) {
     size_t cs = A.n2;
     int i = q % A.nx, j = q / A.nx;
     double y = (A.stf == 1.0) ? (double)j * A.dy : A.dy * (pow(A.stf, (double)j) - 1.0) / (A.stf - 1.0);
-    double yplus = sqrt(A.Re * A.wz[i].x / sqrt(A.fac_y)) * y;
+    double wz0 = (A.damping & 2) ? fabs(A.wz[i].x) : A.wz[i].x;
+    double yplus = sqrt(A.Re * wz0 / sqrt(A.fac_y)) * y;
     double damp;
-    if (A.damping == 1) {
+    if (A.damping & 1) {
         double e = 1.0 - exp(-yplus / A.Aplus);
         damp = e * e;
     } else {
