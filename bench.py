@@ -138,6 +138,14 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def resident_gb():
+    """Device memory in use on this GPU (the fields, multigrid levels and
+    scratch of the live contexts, plus the CUDA context), GB."""
+    import torch
+    free, total = torch.cuda.mem_get_info()
+    return (total - free) / 1e9
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -343,6 +351,45 @@ def plain_comparison(coefs, base, mixed_state2, t0, hbm_peak):
             "fp64_rerun": rerun}
 
 
+def config5_fp64_check(t0):
+    """Config 5's physics (LES with y+ from |wall vorticity|, the roughness
+    element, TS and oblique forcing at 3e-3) at config 2's x spacing: nx=1025
+    over the same 12 wavelengths, 257 rows, 64 modes.  The mixed form against
+    the plain FP64 form, 2 steps from the same disturbed state, the plain
+    form's solves at 1e-8 with up to 60 V-cycles.  At config 5's own spacing
+    the reference's multigrid diverges on the low modes, so the FP64 form has
+    no converged answer there."""
+    from trans_bl_gb300 import api, configs
+    out, states, base = {}, {}, None
+    for form, prec in (("mixed", api.FORM_MIXED), ("plain", api.FORM_PLAIN_FP64)):
+        cfg = configs.config5(nx=1025, precision=prec)
+        if form == "plain":
+            cfg.max_vcycles = 60
+        coefs, base = configs.setup_inputs(cfg)
+        ctx = api.Context(cfg, coefs, base)
+        ctx.put_state(start_state(cfg, base))
+        vc = []
+        t1 = time.perf_counter()
+        for q in range(2):
+            ctx.step(t0 + q)
+            vc.append(int(np.max(ctx.poisson_stats()["vcycles"][:cfg.kfour])))
+        ctx.synchronize()
+        ps = ctx.poisson_stats()
+        out[form] = {"s_per_step_host": (time.perf_counter() - t1) / 2,
+                     "max_vcycles_last_solve_of_step": vc,
+                     "max_residual_last_solve": float(max(ps["residual"][:cfg.kfour]))}
+        states[form] = ctx.get_state()
+        ctx.close()
+    sm, sp = states["mixed"], states["plain"]
+    out["what"] = ("config 5 physics at nx=1025 (config 2's x spacing), ny=257, 64 modes: mixed form (tolerance "
+                   "1e-8) against the plain FP64 form (1e-8, up to 60 V-cycles), 2 steps from the same state")
+    out["mixed_vs_plain_rel_err"] = {n: float(np.max(np.abs(sm[n] - sp[n])) / max(np.max(np.abs(sp[n])), 1e-300))
+                                     for n in NAMES}
+    out["disturbance_amplitude_rel_err"] = disturbance_amplitude_error(sm, sp, base)
+    out["finite"] = bool(all(np.all(np.isfinite(sm[n])) for n in NAMES))
+    return out
+
+
 def disturbance_amplitude_error(a, b, base):
     """Relative error of the disturbance amplitude A(x) = max_y |u'(x, y)| of
     states a against b, for ux and uy in mode 0 (2D, u' = u - base flow) and
@@ -473,7 +520,7 @@ def main():
             "config": {"workload": workload_name(cfg),
                        "form": (form + "+learned (gated)") if learned else form, "replicas": world,
                        "step": "replayed CUDA graph" if (cfg.step_graph and form == "mixed") else "host-launched kernels",
-                       "l2": "inputs larger than L2: working set ~5 GB vs 129 MB L2",
+                       "l2": "inputs larger than L2: working set ~%.0f GB vs 129 MB L2" % resident_gb(),
                        "start": "disturbed state (1e-3) past the forcing ramp",
                        "launch_shapes": {k: tune[k] for k in ("xline_warps", "yline_threads", "nl_blocks_per_sm",
                                                               "plain_line_warps_multi", "plain_line_warps_single")
@@ -488,7 +535,9 @@ def main():
         t += max(1, min(args.steps, 5)) + 1
     st = ctx.get_state()
     ctx.close()
-    if rank == 0 and world == 1 and form == "mixed" and not args.no_plain and state2 is not None:
+    if rank == 0 and world == 1 and form == "mixed" and not args.no_plain and WORKLOAD["name"] == "config5":
+        line["fp64_check"] = config5_fp64_check(t0)
+    elif rank == 0 and world == 1 and form == "mixed" and not args.no_plain and state2 is not None:
         line["plain_fp64"] = plain_comparison(coefs, base, state2, t0, hbm_peak)
         line["speedup_vs_plain"] = value / line["plain_fp64"]["value"]
         # the metric's error bound: TS-disturbance amplitude of the timed form

@@ -1099,7 +1099,9 @@ void les_terms_impl(ora_ctx* o, C* Fx, C* Fy, C* Fz) {
                     double e = 1.0 - std::exp(-yplus / o->cfg.A_plus);
                     damp = e * e;
                 } else {
-                    double ratio = std::min(yplus / o->cfg.A_plus, 100.0);
+                    // min(y+/A, 100): fmin's IEEE minNum gives 100 for a NaN y+
+                    // (Fortran leaves MIN with a NaN argument unspecified)
+                    double ratio = std::fmin(yplus / o->cfg.A_plus, 100.0);
                     ratio = powi(ratio, 3);
                     damp = 1.0 - std::exp(-ratio);
                 }

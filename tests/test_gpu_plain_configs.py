@@ -57,6 +57,60 @@ def test_poi_uy_at_benchmark_grids(oracle_built, which):
     o.close()
 
 
+def rows257(n_lambda, cap):
+    from trans_bl_gb300 import api, configs
+    cfg = configs.blasius_ts_config(513, 257, 4, 8, 4, n_lambda=n_lambda, amp2d=3e-3, amp3d=3e-3, tol=1e-8,
+                                    max_vcycles=cap, precision=api.FORM_PLAIN_FP64)
+    coefs, base = configs.setup_inputs(cfg)
+    return cfg, coefs, base
+
+
+def solve_both(ora, cfg, coefs, base, seed):
+    from trans_bl_gb300 import api
+    st = disturbed(cfg, base, seed)
+    g = api.Context(cfg, coefs, base)
+    o = ora.Oracle(cfg, coefs, base)
+    g.put_state(st)
+    o.put_state(st)
+    d = o.outuy()
+    g.outuy()
+    g.poi_uy(d, cfg.tol_stage)
+    o.poi_uy(d, cfg.tol_stage)
+    ps = g.poisson_stats()
+    vo, ro = o.poisson_stats()
+    out = (ps["vcycles"][:cfg.kfour], vo, np.array(ps["residual"][:cfg.kfour]), ro,
+           g.get_state()["uy"], o.get_state()["uy"])
+    g.close()
+    o.close()
+    return out
+
+
+def test_poi_uy_257_rows(oracle_built):
+    """Config 5's 257-row wall-normal grid (first cell 0.005 delta*) on 513
+    points over 6 wavelengths (config 2's x spacing), 4 modes: one solve at
+    tolerance 1e-8 (about 20 V-cycles, cap 30); equal V-cycle counts per mode
+    and uy within 1e-10 relative."""
+    cfg, coefs, base = rows257(6.0, 30)
+    vg, vo, rg, ro, ug, uo = solve_both(oracle_built, cfg, coefs, base, 23)
+    print("\n257 rows: V-cycles GPU %s oracle %s" % (vg, vo))
+    assert vg == vo
+    assert max(vg) < cfg.max_vcycles
+    assert rel(ug, uo) < 1e-10
+
+
+def test_config5_spacing_diverges_in_both(oracle_built):
+    """At config 5's x spacing (2049 points over 12 wavelengths: 513 over 3)
+    the reference's multigrid diverges on the low modes, the largest
+    wall-normal spacing being ~5.6 dx; the GPU's plain form diverges alike:
+    both stop at the cap of 11 with the same defects to within a factor 2."""
+    cfg, coefs, base = rows257(3.0, 11)
+    vg, vo, rg, ro, ug, uo = solve_both(oracle_built, cfg, coefs, base, 23)
+    print("\nconfig-5 spacing: residual GPU %s oracle %s" % (rg, ro))
+    assert vg == vo
+    assert vg[0] == 11 and ro[0] > 1e3 * cfg.tol_stage
+    assert 0.5 < rg[0] / ro[0] < 2.0
+
+
 def test_config2_step(oracle_built):
     """One RK4 step (four stages, filter in the fourth) of config 2 from a
     disturbed state past the forcing ramp: every field within 1e-10."""

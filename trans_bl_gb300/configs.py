@@ -75,7 +75,7 @@ def config2(**kw):
     return blasius_ts_config(1025, 193, 32, 64, 4, **kw)
 
 
-def config5(**kw):
+def config5(nx=2049, **kw):
     """Large 3D run with a roughness element and LES: nx=2049, ny=257 (1.02
     stretching to 40 delta*), 64 modes (P=128), 4-level multigrid; 2D TS wave
     plus the oblique pair at amplitude 3e-3; Smagorinsky LES (drv_les,
@@ -96,12 +96,16 @@ def config5(**kw):
     negative within the first step, where the reference's sqrt(Re wz_wall)
     (les_par.f:194) is NaN.  The Poisson tolerance defaults to 1e-8: on this
     grid the FP64 defect itself carries round-off of ~6e-9 (first cell
-    0.005 delta*), so 1e-10 is not reachable in FP64."""
+    0.005 delta*), so 1e-10 is not reachable in FP64.
+
+    nx other than 2049 keeps the 12 wavelengths (nx=1025: config 2's x
+    spacing, where the reference's plain multigrid still converges on this
+    wall-normal grid; at 2049 points it diverges on the low modes)."""
     kw.setdefault("tol", 1e-8)
     kw.setdefault("amp2d", 3e-3)
     kw.setdefault("amp3d", 3e-3)
     kw.setdefault("my_form", 4)
-    cfg = blasius_ts_config(2049, 257, 64, 128, 4, **kw)
+    cfg = blasius_ts_config(nx, 257, 64, 128, 4, **kw)
     if "steps_per_period" not in kw:
         cfg.stpp = stable_steps_per_period(cfg)
     dstar = BLASIUS_DSTAR / math.sqrt(cfg.Re)
