@@ -60,7 +60,7 @@ def test_poi_uy_at_benchmark_grids(oracle_built, which):
 def rows257(n_lambda, cap):
     from trans_bl_gb300 import api, configs
     cfg = configs.blasius_ts_config(513, 257, 4, 8, 4, n_lambda=n_lambda, amp2d=3e-3, amp3d=3e-3, tol=1e-8,
-                                    max_vcycles=cap, precision=api.FORM_PLAIN_FP64)
+                                    max_vcycles=cap, precision=api.FORM_PLAIN_FP64, strip=(0.5, 1.0))
     coefs, base = configs.setup_inputs(cfg)
     return cfg, coefs, base
 
