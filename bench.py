@@ -503,11 +503,12 @@ def main():
         r_ms, r_n = fam["relax0"]
         kernel = "k_relax (finest level, one warp per y-line and mode)"
         achieved = bytes_per_launch / (r_ms * 1e-3 / max(r_n, 1)) / 1e9 if r_n else 0.0
-        # DRAM bytes (read + write) per launch from an ncu capture of this command:
-        # the centre-colour launches of the 513-point level read 1.07x their
-        # algorithmic bytes and write none back while running; scaled by lines to
-        # the finest level of the config-2 workload
-        traffic = 1.07 * bytes_per_launch if WORKLOAD["name"] == "config2" else None
+        # DRAM bytes (read + write) per launch, averaged over a finest-level
+        # sweep's 4 launches like the algorithmic bytes, from an ncu capture of
+        # this workload: 1.0 MB (border lines) + 3 x 53.6 MB (centre colours) per
+        # sweep = 0.80 of the algorithmic bytes (the lines the previous colour
+        # wrote are still in L2)
+        traffic = 0.80 * bytes_per_launch if WORKLOAD["name"] == "config2" else None
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "traffic": traffic, "peak_source": peak_kind, "kernel": kernel,
                 "algorithmic_bytes_per_launch": bytes_per_launch, "kernel_ms_total": r_ms, "kernel_launches": r_n,
