@@ -54,7 +54,8 @@ typedef struct tb_config {
     int    kfour;       /* stored Fourier modes K (k = 0..K-1)         par.for:106  */
     int    kphys;       /* physical z points P, power of two, >= 4     par.for:106  */
     int    msh;         /* multigrid levels                            par.for:102  */
-    int    my_form;     /* 0: drv_fi (+optional IBM), 4: drv_les       par.for:14   */
+    int    my_form;     /* 0: drv_fi (+optional IBM), 1: drv_gv (linear about the base
+                           flow, Goertler curvature; gv_pert forcing), 4: drv_les  par.for:14 */
     int    i0, i1, i2, i3, i4;  /* buffer ramp end, TS strip, damping  par.for:21,88 */
     int    stpp;        /* time steps per forcing period               par.for:92   */
     int    max_vcycles; /* V-cycle cap (11 in the reference)  poisson_par.f:33      */
@@ -96,6 +97,9 @@ typedef struct tb_config {
     int    forced_mode[4];      /* 0-based Fourier mode index                       */
     double forced_amp[4];       /* amplitude A_k                                    */
     double forced_phase[4];     /* phase phi_k (0 in the reference)                 */
+    /* my_form 1: Goertler number Go of the wall curvature, varg = Go^2 / sqrt(Re)
+       at every point (init_gv, main_par.f:944-970; 0 in the reference)             */
+    double go_number;
 } tb_config;
 
 typedef struct tb_ctx tb_ctx;

@@ -148,6 +148,9 @@ class Oracle:
         if init:
             self.lib.ora_init_fields(self.h)
 
+    def init_fields(self):
+        self.lib.ora_init_fields(self.h)
+
     def close(self):
         if self.h:
             self.lib.ora_destroy(self.h)

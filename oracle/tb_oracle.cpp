@@ -61,8 +61,9 @@ struct ora_ctx {
     // LHS of the compact schemes (derivs_par.f:6-29)
     std::vector<double> a1x, b1x, c1x, a2x, b2x, c2x, a1y, b1y, c1y, a2y, b2y, c2y, a1fv, b1fv, c1fv;
     std::vector<double> afil, bfil, cfil;
-    std::vector<double> bdfc;            // (imax) ramp, bdfc(1,:) == bdfc(2,:) for form 0/4
+    std::vector<double> bdfc, bdfc2;     // (imax) ramps bdfc(1,:), bdfc(2,:) (equal but for form 1)
     std::vector<double> fcx, fcllx;      // (i2)
+    std::vector<double> fcx2, fcllx2;    // (nx) Goertler strip (var_gv)
     std::vector<double> gibbs;           // (kfour)
     std::vector<double> delta_no;        // (nx, ny, kphys)
     std::vector<double> uxb, uyb, wzb, duexmdx;
@@ -825,7 +826,7 @@ void bzone_impl(ora_ctx* o) {  // loop_par.f:6-45
         for (int j = 2; j <= o->ny; j++)
             for (int i = 1; i <= o->nx; i++) {
                 size_t q = o->id(i, j, k);
-                double bd = o->bdfc[i - 1];
+                double bd = (k == 3) ? o->bdfc2[i - 1] : o->bdfc[i - 1];   // bdt = 2 for k = 3
                 o->wx[q] = o->wx[q] * bd;
                 o->wy[q] = o->wy[q] * bd;
                 if ((o->cfg.my_form == 0 || o->cfg.my_form == 4) && k == 1) {
@@ -840,7 +841,7 @@ void bzonew_impl(ora_ctx* o) {  // loop_par.f:691-725
     for (int k = 1; k <= o->K; k++)
         for (int i = 1; i <= o->nx; i++) {
             size_t q = o->id(i, 1, k);
-            double bd = o->bdfc[i - 1];
+            double bd = (k == 3) ? o->bdfc2[i - 1] : o->bdfc[i - 1];
             o->wx[q] = o->wx[q] * bd;
             o->wy[q] = o->wy[q] * bd;
             if ((o->cfg.my_form == 0 || o->cfg.my_form == 4) && k == 1) {
@@ -1053,6 +1054,64 @@ void ts_pert_impl(ora_ctx* o, int t, double tempt) {  // main_par.f:1613-1685
     }
 }
 
+void gv_pert_impl(ora_ctx* o, int t) {  // main_par.f:1577-1610
+    const tb_config& c = o->cfg;
+    double A = 1e-6 * std::sqrt(o->fac_y);
+    if (t < c.stpp) {
+        double ep = (double)t / (double)c.stpp;
+        A = A * ((6.0 * ep - 15.0) * ep + 10.0) * powi(ep, 3);
+    }
+    for (int i = c.i1 + 1; i <= c.i2 - 1; i++)
+        for (int k = 2; k <= o->K; k++) {
+            o->uy[o->id(i, 1, k)] = mk(A * o->fcx2[i - 1], 0.0);
+            o->d2uydx2[(size_t)(i - 1) + (size_t)o->nx * (k - 1)] = mk(A * o->fcllx2[i - 1], 0.0);
+        }
+}
+
+// lterms_gv (nlterms_par.f:89-112) and drv_gv (main_par.f:1338-1401): the
+// linearised terms about the 2D base flow and the curvature terms, with
+// varg = Go^2 / sqrt(Re) at every point; dvargdx, its compact x-derivative,
+// is zero for the constant varg and is left out.
+void drv_gv_impl(ora_ctx* o, C* dvx, C* dvy, C* dvz) {
+    size_t N3 = o->N3();
+    std::vector<C> a(N3), b(N3), c(N3), d(N3), dadx(N3), dbdx(N3), dddx(N3), dady(N3), dcdy(N3);
+    std::vector<C> xx[3] = {std::vector<C>(N3), std::vector<C>(N3), std::vector<C>(N3)};
+    std::vector<C> yy[3] = {std::vector<C>(N3), std::vector<C>(N3), std::vector<C>(N3)};
+    for (int k = 1; k <= o->K; k++)
+        for (int j = 1; j <= o->ny; j++)
+            for (int i = 1; i <= o->nx; i++) {
+                size_t q = o->id(i, j, k), p = o->id2(i, j);
+                double U = o->uxb[p], V = o->uyb[p], W = o->wzb[p];
+                a[q] = V * o->wx[q] - o->wy[q] * U;
+                b[q] = U * o->wz[q] + o->ux[q] * W;
+                c[q] = -V * o->wz[q] - o->uy[q] * W;
+                d[q] = 2.0 * U * o->ux[q];
+            }
+    derparx_impl(o, dadx.data(), a.data());
+    derparx_impl(o, dbdx.data(), b.data());
+    derparx_impl(o, dddx.data(), d.data());
+    dery_impl(o, dady.data(), a.data(), 0);
+    dery_impl(o, dcdy.data(), c.data(), 0);
+    derparxx_impl(o, xx[0].data(), o->wx.data());
+    derparxx_impl(o, xx[1].data(), o->wy.data());
+    derparxx_impl(o, xx[2].data(), o->wz.data());
+    dery_impl(o, yy[0].data(), o->wx.data(), 2);
+    dery_impl(o, yy[1].data(), o->wy.data(), 2);
+    dery_impl(o, yy[2].data(), o->wz.data(), 2);
+    const double Re = o->Re, fy = o->fac_y, varg = o->cfg.go_number * o->cfg.go_number / std::sqrt(Re);
+    for (int k = 1; k <= o->K; k++) {
+        C vkb = o->v_kb[k - 1];
+        double k2 = o->v_k2b2[k - 1];
+        for (int j = 2; j <= o->ny; j++)
+            for (int i = 1; i <= o->nx; i++) {
+                size_t q = o->id(i, j, k);
+                dvx[q] = -dady[q] + vkb * b[q] - vkb * d[q] * varg + (xx[0][q] + yy[0][q] * fy + k2 * o->wx[q]) / Re;
+                dvy[q] = -(vkb * c[q]) + dadx[q] + (xx[1][q] + yy[1][q] * fy + k2 * o->wy[q]) / Re;
+                dvz[q] = -dbdx[q] + dcdy[q] + varg * dddx[q] + (xx[2][q] + yy[2][q] * fy + k2 * o->wz[q]) / Re;
+            }
+    }
+}
+
 // les_par.f:6-211 (terms whose results the reference never uses -- the
 // x/y/z derivatives of nu_t and the nu_t spectrum -- are not formed).
 void les_terms_impl(ora_ctx* o, C* Fx, C* Fy, C* Fz) {
@@ -1145,6 +1204,7 @@ void cvirt_impl(ora_ctx* o, C* Fx, C* Fy, C* Fz) {  // immersed_par.f:262-313
     }
 }
 void drv_impl(ora_ctx* o, C* dvx, C* dvy, C* dvz) {  // main_par.f:1264-1336 / 1487-1574
+    if (o->cfg.my_form == 1) { drv_gv_impl(o, dvx, dvy, dvz); return; }
     size_t N3 = o->N3();
     std::vector<C> a(N3), b(N3), c(N3), dadx(N3), dbdx(N3), dady(N3), dcdy(N3);
     std::vector<C> xx[3] = {std::vector<C>(N3), std::vector<C>(N3), std::vector<C>(N3)};
@@ -1306,6 +1366,22 @@ void setup_constants(ora_ctx* o) {
         o->bdfc[i - 1] = powi(1.0 - powi(ep, 50), 4) * std::exp(-powi(ep, 4) / 10.0);
     }
     for (int i = c.i4; i <= nx; i++) o->bdfc[i - 1] = 0.0;
+    // bdfc(2,:): init_gv's ramp over i = 1 .. 2 (i1 + i2) (main_par.f:991-996)
+    o->bdfc2 = o->bdfc;
+    if (c.my_form == 1) {
+        int igv = std::min(2 * (c.i1 + c.i2), nx);
+        for (int i = 1; i <= igv; i++) {
+            double ep = (double)(i - 1) / (double)(igv - 1);
+            o->bdfc2[i - 1] = ((6.0 * ep - 15.0) * ep + 10.0) * powi(ep, 3);
+        }
+    }
+    // var_gv (main_par.f:1739-1759)
+    o->fcx2.assign(nx, 0.0); o->fcllx2.assign(nx, 0.0);
+    for (int i = c.i1; i <= c.i2 && i <= nx; i++) {
+        double x = PI * (double)(i - c.i1) / (double)(c.i2 - c.i1);
+        o->fcx2[i - 1] = powi(std::sin(x), 3);
+        o->fcllx2[i - 1] = 6.0 * powi(std::cos(x), 2) * std::sin(x) - 3.0 * powi(std::sin(x), 3);
+    }
     // gibbs_function (immersed_par.f:205-259): final form exp(-theta^2)
     o->gibbs.assign(o->K, 1.0);
     for (int k = 1; k <= o->K; k++) {
@@ -1423,6 +1499,7 @@ int ora_init_fields(ora_ctx* o) {  // main_par.f:601-641
                     &o->dv2x, &o->dv2y, &o->dv2z, &o->fx, &o->fy, &o->fz})
         std::fill(v->begin(), v->end(), mk(0, 0));
     std::fill(o->d2uydx2.begin(), o->d2uydx2.end(), mk(0, 0));
+    if (o->cfg.my_form == 1) return 0;   // init_gv: every mode a disturbance, all zero
     for (int j = 1; j <= o->ny; j++)
         for (int i = 1; i <= o->nx; i++) {
             o->ux[o->id(i, j, 1)] = mk(o->uxb[o->id2(i, j)], 0.0);
@@ -1469,7 +1546,11 @@ int ora_poi_ux(ora_ctx* o, double* d) { poi_ux_impl(o, AS_C(d)); return 0; }
 int ora_poi_uz(ora_ctx* o, const double* d) { poi_uz_impl(o, AS_CC(d)); return 0; }
 int ora_wx_wall(ora_ctx* o, double* l) { wx_wall_impl(o, AS_C(l)); return 0; }
 int ora_wz_wall(ora_ctx* o, const double* l) { wz_wall_impl(o, AS_CC(l)); return 0; }
-int ora_ts_pert(ora_ctx* o, int t, double tempt) { ts_pert_impl(o, t, tempt); return 0; }
+int ora_ts_pert(ora_ctx* o, int t, double tempt) {
+    if (o->cfg.my_form == 1) gv_pert_impl(o, t);
+    else ts_pert_impl(o, t, tempt);
+    return 0;
+}
 int ora_les_terms(ora_ctx* o, double* x, double* y, double* z) { les_terms_impl(o, AS_C(x), AS_C(y), AS_C(z)); return 0; }
 int ora_cvirt(ora_ctx* o, double* x, double* y, double* z) { cvirt_impl(o, AS_C(x), AS_C(y), AS_C(z)); return 0; }
 int ora_loop(ora_ctx* o, double erro) { loop_impl(o, erro, erro < 1.0e-5); return 0; }
@@ -1505,8 +1586,10 @@ int ora_rk_stage(ora_ctx* o, int stage, int t) {
                     o->wz[q] = o->wz1[q] + o->dt6 * (d1z[q] + d2z[q]);
                 }
             }
-    if (stage == 1) ts_pert_impl(o, t, 0.5);
-    if (stage == 3) ts_pert_impl(o, t, 1.0);
+    if (stage == 1 || stage == 3) {
+        if (c.my_form == 1) gv_pert_impl(o, t);
+        else ts_pert_impl(o, t, stage == 1 ? 0.5 : 1.0);
+    }
     if (stage < 4) loop_impl(o, c.tol_stage, false);
     else loop_impl(o, c.tol_final, true);
     return 0;

@@ -103,3 +103,31 @@ def test_les_damping_reversed_wall_shear(lib_built, oracle_built, damping):
     finite = all(np.all(np.isfinite(a)) for a in out[damping, "neg"])
     assert finite == (damping == 0)
     assert all(np.all(np.isfinite(a)) for a in out[damping + 2, "neg"])
+
+
+def test_gortler_form_is_linear(lib_built, oracle_built):
+    """drv_gv is linear in the disturbance (the base flow is fixed): drv of
+    2s is twice drv of s; the curvature terms enter dvx and dvz only; the
+    form starts from zero fields and gv_pert forces modes k >= 1 only."""
+    from trans_bl_gb300 import configs
+    out = {}
+    for go in (0.0, 8.0):
+        cfg = configs.gortler(go_number=go, make_default=oracle_built.default_config)
+        coefs, base = oracle_built.setup_inputs(cfg)
+        o = oracle_built.Oracle(cfg, coefs, base)
+        s = configs.disturbance_state(cfg, np.random.default_rng(56))
+        o.put_state(s)
+        d1 = o.drv()
+        o.put_state({n: 2.0 * f for n, f in s.items()})
+        d2 = o.drv()
+        for a, b in zip(d1, d2):
+            assert rel(b, 2.0 * a) < 1e-12
+        out[go] = d1
+        o.init_fields()
+        z = o.get_state()
+        assert all(np.all(f == 0) for f in z.values())
+        o.ts_pert(cfg.stpp + 1, 0.5)
+        uy = o.get_state()["uy"]
+        assert np.all(uy[0] == 0) and np.max(np.abs(uy[1:, 0, :])) > 0
+    assert np.array_equal(out[0.0][1], out[8.0][1])
+    assert not np.array_equal(out[0.0][0], out[8.0][0]) and not np.array_equal(out[0.0][2], out[8.0][2])

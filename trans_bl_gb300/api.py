@@ -29,7 +29,7 @@ class TbConfig(C.Structure):
             "Re", "dx", "dy", "stf", "x0", "alpha", "omega", "beta", "fac_y", "alphaf", "tol_stage",
             "tol_final", "C_s", "A_plus", "irf", "ibm_xc", "ibm_zc", "ibm_h", "ibm_R")] + \
         [("n_forced", C.c_int), ("forced_mode", C.c_int * 4), ("forced_amp", C.c_double * 4),
-         ("forced_phase", C.c_double * 4)]
+         ("forced_phase", C.c_double * 4), ("go_number", C.c_double)]
 
     def as_dict(self):
         d = {}

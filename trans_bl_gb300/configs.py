@@ -165,6 +165,18 @@ def small(nx=65, ny=33, kfour=4, kphys=8, msh=3, **kw):
     return blasius_ts_config(nx, ny, kfour, kphys, msh, **kw)
 
 
+def gortler(nx=65, ny=33, kfour=4, kphys=8, msh=3, go_number=0.0, **kw):
+    """Goertler form (my_form 1, drv_gv, main_par.f:1338-1401): every Fourier
+    mode a linear disturbance about the 2D base flow, forced by the steady
+    wall strip of gv_pert (modes k >= 1, amplitude 1e-6) over i1..i2, with
+    the wall curvature of Goertler number go_number (0 in the reference).
+    The ramp of the third mode's buffer zone, over i = 1 .. 2 (i1 + i2), is
+    clamped to nx."""
+    cfg = small(nx=nx, ny=ny, kfour=kfour, kphys=kphys, msh=msh, my_form=1, **kw)
+    cfg.go_number = go_number
+    return cfg
+
+
 NAMES = ("ux", "uy", "uz", "wx", "wy", "wz")
 
 
@@ -198,6 +210,16 @@ def disturbed_state(cfg, base, rng, amp=1e-3):
     st["ux"][0] += uxb
     st["uy"][0] += uyb
     st["wz"][0] += wzb
+    return st
+
+
+def disturbance_state(cfg, rng, amp=1e-3):
+    """A smooth seeded disturbance of size amp in every field and mode, no
+    base flow (the Goertler form's state); velocities keep the no-slip wall
+    row."""
+    st = {n: smooth_random((cfg.kfour, cfg.ny, cfg.nx), rng, amp) for n in NAMES}
+    for n in ("ux", "uy", "uz"):
+        st[n][:, 0, :] = 0.0
     return st
 
 

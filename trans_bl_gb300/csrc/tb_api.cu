@@ -35,7 +35,8 @@ int check_cfg(const tb_config* c) {
     if (c->max_vcycles < 1) { tb_set_error("max_vcycles must be >= 1"); return TB_ERR_ARG; }
     if (c->n_forced < 0 || c->n_forced > 4) { tb_set_error("n_forced must be in [0, 4]"); return TB_ERR_ARG; }
     if (c->precision != TB_FORM_PLAIN_FP64 && c->precision != TB_FORM_MIXED) { tb_set_error("unknown precision form"); return TB_ERR_ARG; }
-    if (c->my_form != 0 && c->my_form != 4) { tb_set_error("my_form must be 0 or 4"); return TB_ERR_ARG; }
+    if (c->my_form != 0 && c->my_form != 1 && c->my_form != 4) { tb_set_error("my_form must be 0, 1 or 4"); return TB_ERR_ARG; }
+    if (c->my_form == 1 && c->ibm) { tb_set_error("my_form 1 (drv_gv) has no immersed-boundary term"); return TB_ERR_ARG; }
     if (c->les_damping < 0 || c->les_damping > 3) { tb_set_error("les_damping must be 0..3"); return TB_ERR_ARG; }
     return TB_OK;
 }
@@ -135,7 +136,7 @@ int tb_destroy(tb_ctx* c) {
     tb_mixed_free(c);
     void* ptrs[] = {c->ux, c->uy, c->uz, c->wx, c->wy, c->wz, c->wx1, c->wy1, c->wz1, c->dv1x, c->dv1y, c->dv1z, c->dv2x,
                     c->dv2y, c->dv2z, c->d2uydx2, c->lapv, c->uxb, c->uyb, c->wzb, c->duexmdx, c->bdfc, c->fcx, c->fcllx,
-                    c->gibbs, c->delta_no, c->k2b2, c->tx1.a, c->tx1.g, c->tx1.ib, c->tx2.a, c->tx2.g, c->tx2.ib,
+                    c->fcx2, c->fcllx2, c->gibbs, c->delta_no, c->k2b2, c->tx1.a, c->tx1.g, c->tx1.ib, c->tx2.a, c->tx2.g, c->tx2.ib,
                     c->tfil.a, c->tfil.g, c->tfil.ib,
                     c->tx1.hf, c->tx1.hb, c->tx1.pf, c->tx1.pb, c->tx2.hf, c->tx2.hb, c->tx2.pf, c->tx2.pb,
                     c->tfil.hf, c->tfil.hb, c->tfil.pf, c->tfil.pb,
@@ -203,8 +204,12 @@ int tb_init_fields(tb_ctx* c) {  // main_par.f:601-641
     for (cplx* f : fields) TB_CUDA(cudaMemsetAsync(f, 0, n3 * sizeof(cplx), c->stream));
     TB_CUDA(cudaMemsetAsync(c->d2uydx2, 0, (size_t)c->g.nx * c->g.K * sizeof(cplx), c->stream));
     size_t n2 = tb_n2(c);
-    k_init_mode0<<<tb_blocks(n2, 256), 256, 0, c->stream>>>(c->ux, c->uy, c->wz, c->uxb, c->uyb, c->wzb, n2);
-    TB_CHECK_LAUNCH(c);
+    // forms 0 and 4 carry the base flow in mode 0; the Goertler form's modes
+    // are all disturbances about it (init_gv zeroes every field)
+    if (c->cfg.my_form != 1) {
+        k_init_mode0<<<tb_blocks(n2, 256), 256, 0, c->stream>>>(c->ux, c->uy, c->wz, c->uxb, c->uyb, c->wzb, n2);
+        TB_CHECK_LAUNCH(c);
+    }
     c->inited = true;
     return finish(c);
 }

@@ -453,6 +453,20 @@ int tb_host_build_tables(tb_ctx* c) {
         if ((r = upload(&c->fcx, c->h_fcx))) return r;
         if ((r = upload(&c->fcllx, c->h_fcllx))) return r;
     }
+    // var_gv (main_par.f:1739-1759): the steady Goertler strip sin^3 and its
+    // second x-derivative factor, over i1..i2
+    {
+        int i1 = cf.i1, i2 = cf.i2;
+        c->h_fcx2.assign(nx, 0.0); c->h_fcllx2.assign(nx, 0.0);
+        for (int i = i1; i <= i2 && i <= nx; i++) {
+            double x = PI * (double)(i - i1) / (double)(i2 - i1);
+            double sx = std::sin(x), cx = std::cos(x);
+            c->h_fcx2[i - 1] = sx * sx * sx;
+            c->h_fcllx2[i - 1] = 6.0 * cx * cx * sx - 3.0 * sx * sx * sx;
+        }
+        if ((r = upload(&c->fcx2, c->h_fcx2))) return r;
+        if ((r = upload(&c->fcllx2, c->h_fcllx2))) return r;
+    }
     // buffer ramps (main_par.f:737-756)
     {
         c->h_bdfc.assign(nx, 0.0);
@@ -466,6 +480,18 @@ int tb_host_build_tables(tb_ctx* c) {
             c->h_bdfc[i - 1] = tb_powi(1.0 - tb_powi(ep, 50), 4) * std::exp(-tb_powi(ep, 4) / 10.0);
         }
         for (int i = cf.i4; i <= nx; i++) c->h_bdfc[i - 1] = 0.0;
+        // second row, for mode 2 (bzone's bdt = 2, loop_par.f:19-20): equal to
+        // the first, except in the Goertler form (init_gv, main_par.f:991-996),
+        // where it ramps up over i = 1 .. 2 (i1 + i2)
+        c->h_bdfc.resize(2 * (size_t)nx);
+        for (int i = 0; i < nx; i++) c->h_bdfc[nx + i] = c->h_bdfc[i];
+        if (cf.my_form == 1) {
+            int igv = std::min(2 * (cf.i1 + cf.i2), nx);
+            for (int i = 1; i <= igv; i++) {
+                double ep = (double)(i - 1) / (double)(igv - 1);
+                c->h_bdfc[nx + i - 1] = ((6.0 * ep - 15.0) * ep + 10.0) * tb_powi(ep, 3);
+            }
+        }
         if ((r = upload(&c->bdfc, c->h_bdfc))) return r;
     }
     // gibbs_function final form exp(-theta^2) (immersed_par.f:248-249); K = 1 guarded

@@ -85,7 +85,7 @@ struct tb_ctx {
     std::vector<double> h_qdy, h_qdy2;    // v_qdy(ny), v_qdy2(ny*msh)
     std::vector<double> h_dx2;            // v_dx2(msh)
     std::vector<double> h_k2b2;           // v_k2b2(K)
-    std::vector<double> h_bdfc, h_fcx, h_fcllx, h_gibbs, h_uxb, h_uyb, h_wzb, h_duexmdx;
+    std::vector<double> h_bdfc, h_fcx, h_fcllx, h_fcx2, h_fcllx2, h_gibbs, h_uxb, h_uyb, h_wzb, h_duexmdx;
 
     // device state (comm.var) and RK storage
     cplx *ux = nullptr, *uy = nullptr, *uz = nullptr, *wx = nullptr, *wy = nullptr, *wz = nullptr;
@@ -96,6 +96,7 @@ struct tb_ctx {
     cplx* tmp[24] = {nullptr};   // work fields (nx, ny, K)
     double* uxb = nullptr; double* uyb = nullptr; double* wzb = nullptr; double* duexmdx = nullptr;
     double* bdfc = nullptr; double* fcx = nullptr; double* fcllx = nullptr; double* gibbs = nullptr;
+    double* fcx2 = nullptr; double* fcllx2 = nullptr;   // Goertler strip (var_gv)
     double* delta_no = nullptr;  // (nx, ny, P) IBM indicator
     double* k2b2 = nullptr;      // (K)
     // line-operator tables

@@ -20,10 +20,11 @@ struct CombArgs {
     const cplx *c, *dadx, *xx1, *yy1, *wy;
     const cplx *dbdx, *dcdy, *xx2, *yy2, *wz;
     const cplx *fx, *fy, *dfzdy, *dfzdx, *dfxdy, *dfydx;  // force terms, null if none
+    const cplx *gd, *gdddx;                               // drv_gv's d and dd/dx, null if none
     cplx *dvx, *dvy, *dvz;
     const double* k2b2;
     int nx, ny, K;
-    double beta, invRe, fac_y;
+    double beta, invRe, fac_y, varg;
 };
 __global__ void k_combine(CombArgs A) {
     size_t n = (size_t)A.nx * A.ny * A.K;
@@ -40,6 +41,10 @@ __global__ void k_combine(CombArgs A) {
         vx = cs_(ca(vx, cm(1.0 / fy, ikb(kb, A.fy[q]))), A.dfzdy[q]);
         vy = cs_(ca(vy, A.dfzdx[q]), ikb(kb, A.fx[q]));
         vz = cs_(ca(vz, A.dfxdy[q]), cm(1.0 / fy, A.dfydx[q]));
+    }
+    if (A.gd) {   // drv_gv (main_par.f:1382-1396): - v_kb d varg, + varg dd/dx
+        vx = cs_(vx, cm(A.varg, ikb(kb, A.gd[q])));
+        vz = ca(vz, cm(A.varg, A.gdddx[q]));
     }
     A.dvx[q] = vx; A.dvy[q] = vy; A.dvz[q] = vz;
 }
@@ -79,7 +84,8 @@ __global__ void k_rk(RkArgs A) {
     }
 }
 
-// bzone (loop_par.f:6-45) for j >= 2 and bzonew (691-725) for j = 1.
+// bzone (loop_par.f:6-45) for j >= 2 and bzonew (691-725) for j = 1; bdfc
+// holds the two ramp rows bdfc(1,:), bdfc(2,:) one after the other.
 __global__ void k_bzone(cplx* wx, cplx* wy, cplx* wz, const double* bdfc, const double* wzb, int nx, int ny, int K,
                         int wall, int form) {
     size_t n = (size_t)nx * (wall ? 1 : ny) * K;
@@ -89,7 +95,7 @@ __global__ void k_bzone(cplx* wx, cplx* wy, cplx* wz, const double* bdfc, const 
     if (wall) { i = (int)(t % nx); k = (int)(t / nx); j = 0; }
     else { i = (int)(t % nx); j = (int)((t / nx) % ny); k = (int)(t / ((size_t)nx * ny)); if (j < 1) return; }
     size_t q = (size_t)i + (size_t)nx * (j + (size_t)ny * k);
-    double bd = bdfc[i];
+    double bd = bdfc[(k == 2 ? (size_t)nx : 0) + i];   // bdt = 2 for the third mode (loop_par.f:19-20)
     wx[q] = cm(bd, wx[q]);
     wy[q] = cm(bd, wy[q]);
     if ((form == 0 || form == 4) && k == 0) {
@@ -389,12 +395,74 @@ __global__ void k_ts_pert(PertArgs A) {
     }
 }
 
+// lterms_gv (nlterms_par.f:89-112): the disturbance times the 2D base flow,
+// pointwise in every mode.
+__global__ void k_lterms_gv(const cplx* ux, const cplx* uy, const cplx* wx, const cplx* wy, const cplx* wz,
+                            const double* uxb, const double* uyb, const double* wzb, cplx* a, cplx* b, cplx* c,
+                            cplx* d, int nx, int ny, int K) {
+    const size_t n2 = (size_t)nx * ny;
+    const size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q >= n2 * K) return;
+    const size_t p = q % n2;
+    const double U = uxb[p], V = uyb[p], W = wzb[p];
+    const cplx ex = wx[q], ey = wy[q], ez = wz[q], u = ux[q], v = uy[q];
+    a[q] = cs_(cm(V, ex), cm(U, ey));
+    b[q] = ca(cm(U, ez), cm(W, u));
+    c[q] = cs_(cm(-V, ez), cm(W, v));
+    d[q] = cm(2.0 * U, u);
+}
+
+// gv_pert (main_par.f:1577-1610): the steady Goertler strip in every mode
+// k >= 1 (0-based), wall row, 1-based i1+1 .. i2-1; amplitude a (or *a_dev
+// in a recorded step).
+__global__ void k_gv_pert(cplx* uy, cplx* d2uydx2, const double* fcx2, const double* fcllx2, int nx, int ny, int K,
+                          int i1, int i2, double a, const double* a_dev) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t % nx, k = 1 + t / nx;
+    if (k >= K || i < i1 || i > i2 - 2) return;
+    const double A = a_dev ? *a_dev : a;
+    uy[(size_t)i + (size_t)nx * ny * k] = make_double2(A * fcx2[i], 0.0);
+    d2uydx2[(size_t)i + (size_t)nx * k] = make_double2(A * fcllx2[i], 0.0);
+}
+
 }  // namespace
+
+// drv_gv (main_par.f:1338-1401): linear terms about the base flow, their
+// derivatives, the viscous terms and the curvature terms with varg =
+// Go^2 / sqrt(Re) at every point (init_gv, main_par.f:944-970); dvargdx, the
+// compact x-derivative of the constant varg, is zero and left out.
+int tb_drv_gv(tb_ctx* c, cplx* dvx, cplx* dvy, cplx* dvz) {
+    cplx** t = c->tmp;
+    int r;
+    k_lterms_gv<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(c->ux, c->uy, c->wx, c->wy, c->wz, c->uxb, c->uyb,
+                                                                  c->wzb, t[0], t[1], t[2], t[13], c->g.nx, c->g.ny,
+                                                                  c->g.K);
+    TB_CHECK_LAUNCH(c);
+    XJob xj[6] = {{t[0], t[3], XOP_D1}, {t[1], t[4], XOP_D1}, {t[13], t[14], XOP_D1},
+                  {c->wx, t[5], XOP_D2}, {c->wy, t[6], XOP_D2}, {c->wz, t[7], XOP_D2}};
+    YJob yj[5] = {{t[0], t[8], YOP_D1}, {t[2], t[9], YOP_D1},
+                  {c->wx, t[10], YOP_D2}, {c->wy, t[11], YOP_D2}, {c->wz, t[12], YOP_D2}};
+    if ((r = tb_launch_xlines(c, xj, 6))) return r;
+    if ((r = tb_launch_ylines(c, yj, 5))) return r;
+    CombArgs A;
+    std::memset(&A, 0, sizeof A);
+    A.dady = t[8]; A.b = t[1]; A.xx0 = t[5]; A.yy0 = t[10]; A.wx = c->wx;
+    A.c = t[2]; A.dadx = t[3]; A.xx1 = t[6]; A.yy1 = t[11]; A.wy = c->wy;
+    A.dbdx = t[4]; A.dcdy = t[9]; A.xx2 = t[7]; A.yy2 = t[12]; A.wz = c->wz;
+    A.gd = t[13]; A.gdddx = t[14];
+    A.varg = c->cfg.go_number * c->cfg.go_number / std::sqrt(c->cfg.Re);
+    A.dvx = dvx; A.dvy = dvy; A.dvz = dvz; A.k2b2 = c->k2b2;
+    A.nx = c->g.nx; A.ny = c->g.ny; A.K = c->g.K; A.beta = c->cfg.beta; A.invRe = 1.0 / c->cfg.Re; A.fac_y = c->cfg.fac_y;
+    k_combine<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(A);
+    TB_CHECK_LAUNCH(c);
+    return TB_OK;
+}
 
 // ===========================================================================
 int tb_drv_k(tb_ctx* c, cplx* dvx, cplx* dvy, cplx* dvz) {
     cplx** t = c->tmp;
     int r;
+    if (c->cfg.my_form == 1) return tb_drv_gv(c, dvx, dvy, dvz);
     if (c->cfg.my_form == 4 || c->cfg.ibm) {
         cplx* f[3] = {t[16], t[17], t[18]};
         cplx* df[4] = {t[19], t[20], t[21], t[22]};
@@ -560,6 +628,15 @@ int tb_wz_wall_k(tb_ctx* c, const cplx* lapv) {
 // of the forced modes that exist on this grid; returns their number.
 int tb_ts_pert_fct(tb_ctx* c, int t, double tempt, double* out) {
     const tb_config& cf = c->cfg;
+    if (cf.my_form == 1) {   // gv_pert (main_par.f:1577-1600): steady after the ramp
+        double A = 1e-6 * std::sqrt(cf.fac_y);
+        if (t < cf.stpp) {
+            double ep = (double)t / (double)cf.stpp;
+            A = A * ((6.0 * ep - 15.0) * ep + 10.0) * tb_powi(ep, 3);
+        }
+        out[0] = A;
+        return 1;
+    }
     int nf = 0;
     for (int m = 0; m < cf.n_forced && m < 4; m++) {
         int k = cf.forced_mode[m];
@@ -580,6 +657,16 @@ int tb_ts_pert_fct(tb_ctx* c, int t, double tempt, double* out) {
 
 int tb_ts_pert_k(tb_ctx* c, int t, double tempt) {
     const tb_config& cf = c->cfg;
+    if (cf.my_form == 1) {
+        double a = 0.0;
+        tb_ts_pert_fct(c, t, tempt, &a);
+        const double* a_dev = c->capturing ? c->d_fct + (tempt < 0.75 ? 0 : 4) : nullptr;
+        if (c->g.K < 2) return TB_OK;
+        k_gv_pert<<<tb_blocks((size_t)c->g.nx * (c->g.K - 1), 128), 128, 0, c->stream>>>(
+            c->uy, c->d2uydx2, c->fcx2, c->fcllx2, c->g.nx, c->g.ny, c->g.K, cf.i1, cf.i2, a, a_dev);
+        TB_CHECK_LAUNCH(c);
+        return TB_OK;
+    }
     PertArgs A;
     std::memset(&A, 0, sizeof A);
     A.uy = c->uy; A.d2uydx2 = c->d2uydx2; A.fcx = c->fcx; A.fcllx = c->fcllx;
