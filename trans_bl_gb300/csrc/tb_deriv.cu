@@ -138,30 +138,52 @@ __device__ __forceinline__ void xline(const XArgs& A, const TriLHS& TL, const cp
     const TriT<R> T(TL);
     const int lane = threadIdx.x & 31;
     const int S = TL.S, Sp = S | 1, n = A.nx;
-    V* F = reinterpret_cast<V*>(wsm);
-    V* U = F + 32 * Sp;
+    V* F = reinterpret_cast<V*>(wsm);   // the line; the sweeps then overwrite each lane's rows in place
     for (int i = lane; i < n; i += 32) F[(i / S) * Sp + i % S] = to_v<V>(f[i]);
     __syncwarp();
     const SmemLine<V> L{F, S, Sp};
     const int H = (OP == XOP_FILTER) ? 3 : 2;
     const int r0 = lane * S, r1 = min(n, r0 + S);
-    V* Ul = U + lane * Sp;
+    V* Ul = F + lane * Sp;
+    // Before any lane overwrites its rows, each takes what it reads outside
+    // them or ahead of its own sweep: the right-hand sides of its boundary
+    // rows (stencils reaching up to 6 rows in), the first window of its
+    // interior rows, and the H rows after its chunk.
+    const int ib0 = max(r0, H), ie = min(r1, n - H);   // the chunk's interior rows [ib0, ie)
+    V rs0[3], rs1[3], hi[3], w[7];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        rs0[q] = V{0, 0}; rs1[q] = V{0, 0}; hi[q] = V{0, 0};
+        const int e = n - H + q;
+        if (q < H && q >= r0 && q < r1) rs0[q] = xrhs<OP, R>(L, q, n, A);
+        if (q < H && e >= r0 && e < r1) rs1[q] = xrhs<OP, R>(L, e, n, A);
+        if (q < H && r1 + q < n) hi[q] = L[r1 + q];
+    }
+#pragma unroll
+    for (int q = 0; q < 7; q++) w[q] = V{0, 0};
+    if (ib0 < ie) {
+#pragma unroll
+        for (int q = 0; q < 2 * H; q++) w[q] = L[ib0 - H + q];
+    }
+    __syncwarp();
     // forward sweep over the chunk with zero carry-in
     V u = V{0, 0};
-    int i = r0;
-    for (; i < r1 && i < H; i++) {
-        V r = xrhs<OP, R>(L, i, n, A);
-        R a = T.a[i], ib = T.ib[i];
-        u = V{(r.x - a * u.x) * ib, (r.y - a * u.y) * ib};
-        Ul[i - r0] = u;
-    }
-    if (i < r1 && i < n - H) {
-        V w[7];
 #pragma unroll
-        for (int q = 0; q < 2 * H; q++) w[q] = L[i - H + q];
-        int nc = (i + H) / S, no = (i + H) % S;   // chunk slot of row i + H
-        for (; i < r1 && i < n - H; i++) {
-            w[2 * H] = F[nc * Sp + no];
+    for (int q = 0; q < 3; q++)
+        if (q < H && q >= r0 && q < r1) {
+            V r = rs0[q];
+            R a = T.a[q], ib = T.ib[q];
+            u = V{(r.x - a * u.x) * ib, (r.y - a * u.y) * ib};
+            Ul[q - r0] = u;
+        }
+    if (ib0 < ie) {
+        int nc = (ib0 + H) / S, no = (ib0 + H) % S;   // chunk slot of row i + H
+        for (int i = ib0; i < ie; i++) {
+            const int d = i + H - r1;                 // >= 0: row i + H is after the chunk
+            V h = hi[0];
+            if (d == 1) h = hi[1];
+            if (d == 2) h = hi[2];
+            w[2 * H] = (d < 0) ? F[nc * Sp + no] : h;
             if (++no == S) { no = 0; nc++; }
             V r;
             if (OP == XOP_D1) {
@@ -186,11 +208,15 @@ __device__ __forceinline__ void xline(const XArgs& A, const TriLHS& TL, const cp
             for (int q = 0; q < 2 * H; q++) w[q] = w[q + 1];
         }
     }
-    for (; i < r1; i++) {
-        V r = xrhs<OP, R>(L, i, n, A);
-        R a = T.a[i], ib = T.ib[i];
-        u = V{(r.x - a * u.x) * ib, (r.y - a * u.y) * ib};
-        Ul[i - r0] = u;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const int e = n - H + q;
+        if (q < H && e >= r0 && e < r1) {
+            V r = rs1[q];
+            R a = T.a[e], ib = T.ib[e];
+            u = V{(r.x - a * u.x) * ib, (r.y - a * u.y) * ib};
+            Ul[e - r0] = u;
+        }
     }
     // forward carries: true chunk-end values by a scan, carry-in = previous lane's
     V b = (r1 > r0) ? u : V{0, 0};
@@ -228,12 +254,12 @@ __device__ __forceinline__ void xline(const XArgs& A, const TriLHS& TL, const cp
         Ul[q - r0] = V{fma(h, Xin.x, xx.x), fma(h, Xin.y, xx.y)};
     }
     __syncwarp();
-    for (int q = lane; q < n; q += 32) o[q] = to_c(U[(q / S) * Sp + q % S]);
+    for (int q = lane; q < n; q += 32) o[q] = to_c(F[(q / S) * Sp + q % S]);
 }
 
 // One warp per x-line of the batched jobs; lines of modes k >= 1 run in FP32
 // when A.fp32_modes is set (the mixed form: they hold only the disturbance).
-// Shared memory per warp: 2 x 32 x Sp complex FP64 (the FP32 path uses half).
+// Shared memory per warp: 32 x Sp complex FP64 (the FP32 path uses half).
 template <int OP>
 __global__ void __launch_bounds__(64) k_xwarp(XArgs A) {
     extern __shared__ cplx xs[];
@@ -247,7 +273,7 @@ __global__ void __launch_bounds__(64) k_xwarp(XArgs A) {
     const XJob& J = A.job[jb];
     if (J.op != OP) return;
     const int line = (int)(gw - (long)jb * nlines);
-    void* wsm = xs + (size_t)wib * 64 * Sp;
+    void* wsm = xs + (size_t)wib * 32 * Sp;
     const cplx* f = J.src + (size_t)line * n;
     cplx* o = J.dst + (size_t)line * n;
     if (A.fp32_modes && line >= A.ny) xline<OP, float>(A, T, f, o, wsm);   // line / ny = mode k >= 1
@@ -334,7 +360,7 @@ int tb_launch_xlines(tb_ctx* c, const XJob* jobs, int njobs) {
     for (int q = 0; q < njobs; q++) has[jobs[q].op] = true;
     const int WPB = c->tune_xw == 1 ? 1 : 2;   // warps per block (tb_autotune), at most 2 (launch bounds)
     int Sp = c->tx1.S | 1;
-    size_t smem = (size_t)WPB * 64 * Sp * sizeof(cplx);
+    size_t smem = (size_t)WPB * 32 * Sp * sizeof(cplx);
     unsigned nb = tb_blocks(lines, WPB);
     cudaEvent_t ps = nullptr;
     if (tb_prof_begin(c, PROF_XLINES, &ps)) return TB_ERR_CUDA;
