@@ -223,19 +223,32 @@ __global__ void __launch_bounds__(64) k_wz_wall(cplx* wz, const cplx* wx, const 
 //   r_0 = boundary value, r_1 = c12 (e_0 + 10 e_1 + e_2),
 //   r_i = c8 (e_{i-1} + 5.5 e_i + e_{i+1}),  r_{n-2} = c12 (e_{n-1} + 10 e_{n-2} + e_{n-3}),
 //   r_{n-1} = rn,
-// with e in E; the solution (rows 1..n-1) goes to out.
-__device__ void penta_line(const cplx* E, cplx* V, const WarpLine& L, int lane, const double* lu, cplx r0v, cplx rn,
-                           double c12, double c8, cplx* out) {
+// with e in E (overwritten); the solution (rows 1..n-1) goes to out.
+__device__ void penta_line(cplx* E, const WarpLine& L, int lane, const double* lu, cplx r0v, cplx rn, double c12,
+                           double c8, cplx* out) {
     const int n = L.n, r0 = lane * L.S, r1 = min(n, r0 + L.S);
     auto e = [&](int i) { return E[L.slot(i)]; };
-    cplx* Vl = V + lane * L.Sp;
+    cplx* Vl = E + lane * L.Sp;   // the rhs and the solution overwrite this lane's rows of e in place
+    // what the stencils read outside the lane's rows (e(r0-1), e(r1)) and the
+    // rhs of rows 1 and n-2, taken before any lane overwrites its rows
+    const cplx z = make_double2(0.0, 0.0);
+    cplx ep = (r0 >= 1 && r0 < r1) ? e(r0 - 1) : z;
+    const cplx en = (r1 < n && r0 < r1) ? e(r1) : z;
+    cplx v1 = z, vn2 = z;
+    if (1 >= r0 && 1 < r1) { cplx a = e(0), b = e(1), c = e(2); v1 = make_double2(c12 * (a.x + 10.0 * b.x + c.x), c12 * (a.y + 10.0 * b.y + c.y)); }
+    if (n - 2 >= r0 && n - 2 < r1) { cplx a = e(n - 1), b = e(n - 2), c = e(n - 3); vn2 = make_double2(c12 * (a.x + 10.0 * b.x + c.x), c12 * (a.y + 10.0 * b.y + c.y)); }
+    __syncwarp();
     for (int i = r0; i < r1; i++) {
+        const cplx b = Vl[i - r0];   // e(i), not yet overwritten
         cplx v;
         if (i == 0) v = r0v;
-        else if (i == 1) { cplx a = e(0), b = e(1), c = e(2); v = make_double2(c12 * (a.x + 10.0 * b.x + c.x), c12 * (a.y + 10.0 * b.y + c.y)); }
-        else if (i <= n - 3) { cplx a = e(i - 1), b = e(i), c = e(i + 1); v = make_double2(c8 * (a.x + 5.5 * b.x + c.x), c8 * (a.y + 5.5 * b.y + c.y)); }
-        else if (i == n - 2) { cplx a = e(n - 1), b = e(n - 2), c = e(n - 3); v = make_double2(c12 * (a.x + 10.0 * b.x + c.x), c12 * (a.y + 10.0 * b.y + c.y)); }
+        else if (i == 1) v = v1;
+        else if (i <= n - 3) {
+            const cplx a = ep, c = (i + 1 < r1) ? Vl[i + 1 - r0] : en;
+            v = make_double2(c8 * (a.x + 5.5 * b.x + c.x), c8 * (a.y + 5.5 * b.y + c.y));
+        } else if (i == n - 2) v = vn2;
         else v = rn;
+        ep = b;
         Vl[i - r0] = v;
     }
     const double *L1 = lu, *L2 = lu + n, *IU3 = lu + 2 * n, *U4 = lu + 3 * n, *U5 = lu + 4 * n;
@@ -246,7 +259,7 @@ __device__ void penta_line(const cplx* E, cplx* V, const WarpLine& L, int lane, 
                   [=](int i) { return i == 0 ? 1.0 : IU3[i]; });
     __syncwarp();
     for (int i = lane; i < n; i += 32)
-        if (i >= 1) out[i] = V[L.slot(i)];
+        if (i >= 1) out[i] = E[L.slot(i)];
 }
 
 // x-penta Poisson of poi_ux / poi_uz (loop_par.f:519-563, 641-685), one warp
@@ -268,8 +281,7 @@ __global__ void __launch_bounds__(64) k_penta_x(PentaArgs A) {
     const int j = 1 + t % (A.ny - 1), k = 1 + t / (A.ny - 1);
     const int n = A.nx;
     const WarpLine L{n, WarpLine::chunk(n), WarpLine::padded(n)};
-    cplx* E = wsm + (size_t)wib * 64 * L.Sp;
-    cplx* V = E + 32 * L.Sp;
+    cplx* E = wsm + (size_t)wib * 32 * L.Sp;
     size_t base = (size_t)n * (j + (size_t)A.ny * k);
     const cplx* D = A.D + base;
     const cplx* W = A.W + base;
@@ -284,7 +296,7 @@ __global__ void __launch_bounds__(64) k_penta_x(PentaArgs A) {
     const double den = 1.0 / ((double)k * (double)k * A.beta * A.beta);
     cplx v = ikb(kb, W[n - 1]), dn = D[n - 1];
     cplx rn = A.uz ? make_double2((-dn.x + v.x) * den, (-dn.y + v.y) * den) : make_double2((v.x + dn.x) * den, (v.y + dn.y) * den);
-    penta_line(E, V, L, lane, A.lu + (size_t)k * 5 * n, O[0], rn, g * (A.dxx / 12.0), g * (8.0 * A.dxx), O);
+    penta_line(E, L, lane, A.lu + (size_t)k * 5 * n, O[0], rn, g * (A.dxx / 12.0), g * (8.0 * A.dxx), O);
 }
 
 // lapv (loop_par.f:194-205) for every (i, k).
@@ -327,8 +339,7 @@ __global__ void __launch_bounds__(64) k_wx_wall(cplx* wx, const cplx* dwdy, cons
     if (k >= K) return;
     const int n = nx;
     const WarpLine L{n, WarpLine::chunk(n), WarpLine::padded(n)};
-    cplx* E = wsm + (size_t)wib * 64 * L.Sp;
-    cplx* V = E + 32 * L.Sp;
+    cplx* E = wsm + (size_t)wib * 32 * L.Sp;
     const cplx* dw = dwdy + (size_t)nx * k;
     const cplx* LV = lapv + (size_t)nx * k;
     cplx* WX = wx + (size_t)nx * ny * k;  // row j = 1
@@ -368,12 +379,13 @@ __global__ void __launch_bounds__(64) k_wx_wall(cplx* wx, const cplx* dwdy, cons
     const double den = 1.0 / ((double)k * (double)k * beta * beta);
     cplx dd = d2(n - 1), vv = ikb(kb, LV[n - 1]);
     cplx rn = make_double2((dd.x - vv.x) * den, (dd.y - vv.y) * den);
-    penta_line(E, V, L, lane, lu_all + (size_t)k * 5 * n, WX[0], rn, dxx / 12.0, 8.0 * dxx, WX);
+    penta_line(E, L, lane, lu_all + (size_t)k * 5 * n, WX[0], rn, dxx / 12.0, 8.0 * dxx, WX);
 }
 
 // Shared memory of the warp-per-line x kernels (two line buffers per warp).
 constexpr int XW_WARPS = 2;
 size_t xw_smem(int nx) { return (size_t)XW_WARPS * 64 * WarpLine::padded(nx) * sizeof(cplx); }
+size_t xw_smem1(int nx) { return (size_t)XW_WARPS * 32 * WarpLine::padded(nx) * sizeof(cplx); }   // in-place lines
 
 // ts2d_pert / ts3d_pert (main_par.f:1613-1685) for each forced mode.
 struct PertArgs {
@@ -576,8 +588,9 @@ int tb_poi_ux_k(tb_ctx* c, cplx* duydy) {
     PentaArgs A{d2, c->wy, c->ux, c->px.lu, c->g.nx, c->g.ny, c->g.K, 0, c->cfg.dx * c->cfg.dx, c->cfg.beta};
     cudaEvent_t ps = nullptr;
     if ((r = tb_prof_begin(c, PROF_PENTA, &ps))) return r;
-    TB_CUDA(cudaFuncSetAttribute(k_penta_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_penta_x<<<tb_blocks((size_t)(c->g.ny - 1) * (c->g.K - 1), XW_WARPS), 32 * XW_WARPS, sm, c->stream>>>(A);
+    const size_t sp = xw_smem1(c->g.nx);
+    TB_CUDA(cudaFuncSetAttribute(k_penta_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp));
+    k_penta_x<<<tb_blocks((size_t)(c->g.ny - 1) * (c->g.K - 1), XW_WARPS), 32 * XW_WARPS, sp, c->stream>>>(A);
     TB_CHECK_LAUNCH(c);
     return tb_prof_end(c, PROF_PENTA, ps);
 }
@@ -588,11 +601,11 @@ int tb_poi_uz_k(tb_ctx* c, const cplx* duydy) {
     XJob xj[1] = {{c->wy, dwydx, XOP_D1}};
     if ((r = tb_launch_xlines(c, xj, 1))) return r;
     PentaArgs A{dwydx, duydy, c->uz, c->px.lu, c->g.nx, c->g.ny, c->g.K, 1, c->cfg.dx * c->cfg.dx, c->cfg.beta};
-    size_t sm = xw_smem(c->g.nx);
     cudaEvent_t ps = nullptr;
     if ((r = tb_prof_begin(c, PROF_PENTA, &ps))) return r;
-    TB_CUDA(cudaFuncSetAttribute(k_penta_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_penta_x<<<tb_blocks((size_t)(c->g.ny - 1) * (c->g.K - 1), XW_WARPS), 32 * XW_WARPS, sm, c->stream>>>(A);
+    const size_t sp = xw_smem1(c->g.nx);
+    TB_CUDA(cudaFuncSetAttribute(k_penta_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp));
+    k_penta_x<<<tb_blocks((size_t)(c->g.ny - 1) * (c->g.K - 1), XW_WARPS), 32 * XW_WARPS, sp, c->stream>>>(A);
     TB_CHECK_LAUNCH(c);
     return tb_prof_end(c, PROF_PENTA, ps);
 }
@@ -608,7 +621,7 @@ int tb_wx_wall_k(tb_ctx* c, cplx* lapv) {
     cplx* dw = c->tmp[15];
     k_dwydy_wall<<<nb, 128, 0, c->stream>>>(dw, c->wy, dcoef + 9, c->g.nx, c->g.ny, c->g.K, 1.0 / c->cfg.dy);
     TB_CHECK_LAUNCH(c);
-    size_t sm = xw_smem(c->g.nx);
+    size_t sm = xw_smem1(c->g.nx);
     TB_CUDA(cudaFuncSetAttribute(k_wx_wall, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_wx_wall<<<tb_blocks(c->g.K - 1, XW_WARPS), 32 * XW_WARPS, sm, c->stream>>>(c->wx, dw, lapv, c->px.lu, c->g.nx, c->g.ny,
                                                                                  c->g.K, c->cfg.dx, c->cfg.dx * c->cfg.dx,
