@@ -305,29 +305,70 @@ __global__ void __launch_bounds__(128) k_ylines(YArgs A) {
     const TriLHS& T = A.t[OP];
     const YRhs& R = A.r[OP];
     cplx u = make_double2(0.0, 0.0);
-    for (int j = 0; j < ny; j++) {
+    // one row of the forward sweep with its rhs from the tables (boundary rows)
+    auto generic = [&](int j) {
         cplx r = make_double2(0.0, 0.0);
-        int c0 = R.cnt[j], of = R.off[j];
+        const int c0 = R.cnt[j], of = R.off[j];
         const double* w = R.w + 7 * j;
-        if (c0 == 5) {
-            const cplx* p = f + (size_t)(j + of) * s;
-            r = cmul(w[0], p[0]);
-            r = cfma(w[1], p[s], r);
-            r = cfma(w[2], p[2 * s], r);
-            r = cfma(w[3], p[3 * s], r);
-            r = cfma(w[4], p[4 * s], r);
-        } else {
-            for (int m = 0; m < c0; m++) r = cfma(w[m], f[(size_t)(j + of + m) * s], r);
-        }
-        double a = T.a[j], ib = T.ib[j];
+        for (int m = 0; m < c0; m++) r = cfma(w[m], f[(size_t)(j + of + m) * s], r);
+        const double a = T.a[j], ib = T.ib[j];
         u = make_double2((r.x - a * u.x) * ib, (r.y - a * u.y) * ib);
         o[(size_t)j * s] = u;
+    };
+    // The sweeps are sequential in j, so each row's loads are issued YPD rows
+    // ahead into a register ring; the interior rows j = 2 .. ny-3 (five-point
+    // rhs f[j-2 .. j+2], derivs_par.f:400-611) keep their window in registers.
+    constexpr int YPD = 8;
+    generic(0);
+    generic(1);
+    {
+        cplx w0 = f[0], w1 = f[s], w2 = f[2 * s], w3 = f[3 * s];
+        cplx pre[YPD];
+#pragma unroll
+        for (int q = 0; q < YPD; q++) pre[q] = (4 + q < ny) ? f[(size_t)(4 + q) * s] : make_double2(0.0, 0.0);
+        for (int jb = 2; jb < ny - 2; jb += YPD) {
+#pragma unroll
+            for (int q = 0; q < YPD; q++) {
+                const int j = jb + q;
+                if (j < ny - 2) {
+                    const cplx w4 = pre[q];   // row j + 2
+                    const int nr = j + 2 + YPD;
+                    if (nr < ny) pre[q] = f[(size_t)nr * s];
+                    const double* w = R.w + 7 * j;
+                    cplx r = cmul(w[0], w0);
+                    r = cfma(w[1], w1, r);
+                    r = cfma(w[2], w2, r);
+                    r = cfma(w[3], w3, r);
+                    r = cfma(w[4], w4, r);
+                    const double a = T.a[j], ib = T.ib[j];
+                    u = make_double2((r.x - a * u.x) * ib, (r.y - a * u.y) * ib);
+                    o[(size_t)j * s] = u;
+                    w0 = w1; w1 = w2; w2 = w3; w3 = w4;
+                }
+            }
+        }
     }
-    for (int j = ny - 2; j >= 0; j--) {
-        double g = T.g[j + 1];
-        cplx v = o[(size_t)j * s];
-        u = make_double2(v.x - g * u.x, v.y - g * u.y);
-        o[(size_t)j * s] = u;
+    generic(ny - 2);
+    generic(ny - 1);
+    // backward sweep, rows ny-2 .. 0, the forward values read YPD rows ahead
+    {
+        cplx pre[YPD];
+#pragma unroll
+        for (int q = 0; q < YPD; q++) pre[q] = (ny - 2 - q >= 0) ? o[(size_t)(ny - 2 - q) * s] : make_double2(0.0, 0.0);
+        for (int jb = ny - 2; jb >= 0; jb -= YPD) {
+#pragma unroll
+            for (int q = 0; q < YPD; q++) {
+                const int j = jb - q;
+                if (j >= 0) {
+                    const cplx v = pre[q];
+                    const int nr = j - YPD;
+                    if (nr >= 0) pre[q] = o[(size_t)nr * s];
+                    const double g = T.g[j + 1];
+                    u = make_double2(v.x - g * u.x, v.y - g * u.y);
+                    o[(size_t)j * s] = u;
+                }
+            }
+        }
     }
 }
 
