@@ -50,8 +50,10 @@ int dalloc(T** p, size_t n) {
 
 // Host <-> device copies of state fields, queued on the context's stream;
 // readers wait once after all fields (tb_get_state, tb_get_wall).  Measured
-// on a GB300 host: ~200 GB/s each way from page-locked memory, the copy
-// engines' rate, which SM loads over NVLink-C2C did not exceed.
+// on a GB300 host with page-locked buffers (config 2, 608 MB per state):
+// ~208 GB/s host to device and ~80 GB/s device to host; SM loads over
+// NVLink-C2C did not beat the first, and spreading the six fields over
+// three streams changed neither.
 int copy_field(tb_ctx* c, void* dst, const void* src, size_t bytes, bool to_device) {
     TB_CUDA(cudaMemcpyAsync(dst, src, bytes, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, c->stream));
     return TB_OK;
