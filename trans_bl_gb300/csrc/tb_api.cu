@@ -51,9 +51,10 @@ int dalloc(T** p, size_t n) {
 // Host <-> device copies of state fields, queued on the context's stream;
 // readers wait once after all fields (tb_get_state, tb_get_wall).  Measured
 // on a GB300 host with page-locked buffers (config 2, 608 MB per state):
-// ~208 GB/s host to device and ~80 GB/s device to host; SM loads over
-// NVLink-C2C did not beat the first, and spreading the six fields over
-// three streams changed neither.
+// the copy engines move ~208 GB/s host to device and ~78 GB/s device to
+// host (three streams instead of one changed neither); the SMs, loading
+// and storing 16 bytes a thread over NVLink-C2C, ~208 and ~190 GB/s.  So a
+// state whose host buffers the device can address moves by k_copy_state.
 int copy_field(tb_ctx* c, void* dst, const void* src, size_t bytes, bool to_device) {
     TB_CUDA(cudaMemcpyAsync(dst, src, bytes, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, c->stream));
     return TB_OK;
@@ -216,10 +217,47 @@ int tb_init_fields(tb_ctx* c) {  // main_par.f:601-641
     return finish(c);
 }
 
+namespace {
+__global__ void k_copy_state(const double2* __restrict__ src, double2* __restrict__ dst, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        dst[q] = src[q];
+}
+// Device addresses of six page-locked host buffers, if the device can
+// address all of them.
+bool state_mapped(const double* const h[6], void* dv[6]) {
+    for (int f = 0; f < 6; f++) {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, h[f]) != cudaSuccess || at.type != cudaMemoryTypeHost || !at.devicePointer) {
+            cudaGetLastError();   // a pageable pointer is not an error here
+            return false;
+        }
+        dv[f] = at.devicePointer;
+    }
+    return true;
+}
+int copy_state_sm(tb_ctx* c, void* const dv[6], bool to_device) {
+    cplx* const dev[6] = {c->ux, c->uy, c->uz, c->wx, c->wy, c->wz};
+    const size_t n3 = tb_n3(c);
+    for (int f = 0; f < 6; f++) {
+        const double2* src = to_device ? static_cast<const double2*>(dv[f]) : dev[f];
+        double2* dst = to_device ? dev[f] : static_cast<double2*>(dv[f]);
+        k_copy_state<<<4 * c->sm_count, 256, 0, c->stream>>>(src, dst, n3);
+        TB_CHECK_LAUNCH(c);
+    }
+    return TB_OK;
+}
+}  // namespace
+
 int tb_put_state(tb_ctx* c, const double* ux, const double* uy, const double* uz, const double* wx, const double* wy, const double* wz) {
     if (!c || !ux || !uy || !uz || !wx || !wy || !wz) { tb_set_error("null argument"); return TB_ERR_ARG; }
     size_t n3 = tb_n3(c);
     int r;
+    const double* const h[6] = {ux, uy, uz, wx, wy, wz};
+    void* dv[6];
+    if (state_mapped(h, dv)) {
+        if ((r = copy_state_sm(c, dv, true))) return r;
+        return finish(c);
+    }
     if ((r = up(c, c->ux, ux, n3)) || (r = up(c, c->uy, uy, n3)) || (r = up(c, c->uz, uz, n3)) ||
         (r = up(c, c->wx, wx, n3)) || (r = up(c, c->wy, wy, n3)) || (r = up(c, c->wz, wz, n3)))
         return r;
@@ -229,6 +267,12 @@ int tb_get_state(tb_ctx* c, double* ux, double* uy, double* uz, double* wx, doub
     if (!c || !ux || !uy || !uz || !wx || !wy || !wz) { tb_set_error("null argument"); return TB_ERR_ARG; }
     size_t n3 = tb_n3(c);
     int r;
+    const double* const h[6] = {ux, uy, uz, wx, wy, wz};
+    void* dv[6];
+    if (state_mapped(h, dv)) {
+        if ((r = copy_state_sm(c, dv, false))) return r;
+        return finish(c);
+    }
     if ((r = down_async(c, ux, c->ux, n3)) || (r = down_async(c, uy, c->uy, n3)) || (r = down_async(c, uz, c->uz, n3)) ||
         (r = down_async(c, wx, c->wx, n3)) || (r = down_async(c, wy, c->wy, n3)) || (r = down_async(c, wz, c->wz, n3)))
         return r;
