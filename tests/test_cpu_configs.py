@@ -32,3 +32,31 @@ def test_ensemble_members():
     assert len({(c.nx, c.ny, c.kfour) for c in a}) > 6   # uneven sizes
     other = configs.config3(seed=7, precision=api.FORM_MIXED)
     assert [(c.nx, c.ny, c.kfour) for c in other] != [(c.nx, c.ny, c.kfour) for c in a]
+
+
+def test_config5():
+    """2049 x 257 x 64 (P = 128), LES with y+ from |wall vorticity|, the
+    roughness element at a quarter of the domain (0.5 delta* high, 2 delta*
+    across) mid-span, tolerance 1e-8, the step its first cell needs and the
+    immersed-boundary gain below the explicit RK4 limit; nx = 1025 keeps
+    the 12 wavelengths (the FP64 check's grid)."""
+    c = configs.config5(precision=api.FORM_MIXED)
+    assert (c.nx, c.ny, c.kfour, c.kphys, c.msh, c.my_form) == (2049, 257, 64, 128, 4, 4)
+    assert c.les_damping == 3 and c.C_s == 0.1 and c.A_plus == 26.0
+    assert c.tol_stage == c.tol_final == 1e-8
+    assert c.stpp == configs.stable_steps_per_period(c) == 16384
+    dstar = configs.BLASIUS_DSTAR / math.sqrt(c.Re)
+    assert c.ibm == 1 and abs(c.ibm_h - 0.5 * dstar) < 1e-15 and abs(c.ibm_R - dstar) < 1e-15
+    assert abs(c.ibm_xc - (c.x0 + 0.25 * (c.nx - 1) * c.dx)) < 1e-12 and abs(c.ibm_zc - math.pi / c.beta) < 1e-12
+    dt = 2.0 * math.pi / c.omega / c.stpp
+    assert c.irf == -0.1 * c.Re and abs(c.irf) * dt < 2.0
+    assert c.forced_amp[0] == c.forced_amp[1] == 3e-3
+    h = configs.config5(nx=1025, precision=api.FORM_MIXED)
+    assert abs(h.dx - 2.0 * c.dx) < 1e-15 and h.ny == c.ny and h.dy == c.dy
+
+
+def test_gortler_config():
+    """The Goertler form's helper: my_form 1, the curvature's Goertler
+    number, no immersed boundary."""
+    c = configs.gortler(go_number=8.0)
+    assert c.my_form == 1 and c.go_number == 8.0 and c.ibm == 0
