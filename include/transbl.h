@@ -55,7 +55,9 @@ typedef struct tb_config {
     int    kphys;       /* physical z points P, power of two, >= 4     par.for:106  */
     int    msh;         /* multigrid levels                            par.for:102  */
     int    my_form;     /* 0: drv_fi (+optional IBM), 1: drv_gv (linear about the base
-                           flow, Goertler curvature; gv_pert forcing), 4: drv_les  par.for:14 */
+                           flow, Goertler curvature; gv_pert forcing), 2: drv_gvth (the
+                           nonlinear disturbance about the base flow with a transported
+                           temperature th), 4: drv_les                        par.for:14 */
     int    i0, i1, i2, i3, i4;  /* buffer ramp end, TS strip, damping  par.for:21,88 */
     int    stpp;        /* time steps per forcing period               par.for:92   */
     int    max_vcycles; /* V-cycle cap (11 in the reference)  poisson_par.f:33      */
@@ -100,6 +102,8 @@ typedef struct tb_config {
     /* my_form 1: Goertler number Go of the wall curvature, varg = Go^2 / sqrt(Re)
        at every point (init_gv, main_par.f:944-970; 0 in the reference)             */
     double go_number;
+    /* my_form 2: Prandtl number of the temperature equation (0.72, par.for:38)   */
+    double Pr;
 } tb_config;
 
 typedef struct tb_ctx tb_ctx;
@@ -172,6 +176,12 @@ int tb_get_state(tb_ctx* ctx, double* ux, double* uy, double* uz,
                  double* wx, double* wy, double* wz);
 /* d2uydx2(nx, K) wall forcing curvature (common /derw/). */
 int tb_put_wall(tb_ctx* ctx, const double* d2uydx2);
+/* my_form 2 only: the base temperature thb(nx,ny) (/blast/, read with the base
+   flow in init_gvth, main_par.f:1125) and the temperature disturbance
+   th(nx,ny,kfour) (complex, comm.var), host pointers. */
+int tb_set_baseflow_th(tb_ctx* ctx, const double* thb);
+int tb_put_th(tb_ctx* ctx, const double* th);
+int tb_get_th(tb_ctx* ctx, double* th);
 int tb_get_wall(tb_ctx* ctx, double* d2uydx2);
 int tb_synchronize(tb_ctx* ctx);
 

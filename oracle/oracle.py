@@ -52,6 +52,8 @@ def load():
     lib.ora_wx_wall.argtypes = [P, D]
     lib.ora_wz_wall.argtypes = [P, D]
     lib.ora_ts_pert.argtypes = [P, C.c_int, C.c_double]
+    for n in ("ora_set_baseflow_th", "ora_put_th", "ora_get_th"):
+        getattr(lib, n).argtypes = [P, D]
     lib.ora_loop.argtypes = [P, C.c_double]
     lib.ora_rk_stage.argtypes = [P, C.c_int, C.c_int]
     lib.ora_step.argtypes = [P, C.c_int]
@@ -76,7 +78,7 @@ def default_config(**kw):
              Re=5.0 * 0.1 / 1.509479531e-5, dx=0.02962963, dy=0.15 / 182.0, stf=1.0, x0=1.0, alpha=0.45723605,
              omega=2.6, beta=34.9, fac_y=1.0, alphaf=0.48, tol_stage=1e-5, tol_final=1e-6, C_s=0.032, A_plus=25.0,
              ibm_xc=1.7, ibm_zc=0.0, ibm_h=0.0, ibm_R=1e-2 / 0.1, n_forced=1, forced_mode=[0], forced_amp=[1e-5],
-             forced_phase=[0.0])
+             forced_phase=[0.0], go_number=0.0, Pr=0.72)
     d["irf"] = -0.1 * d["Re"]
     d.update(kw)
     for k, v in d.items():
@@ -150,6 +152,19 @@ class Oracle:
 
     def init_fields(self):
         self.lib.ora_init_fields(self.h)
+
+    def set_baseflow_th(self, thb):
+        a = np.ascontiguousarray(thb, dtype=np.float64)
+        self.lib.ora_set_baseflow_th(self.h, _d(a))
+
+    def put_th(self, th):
+        a = np.ascontiguousarray(th, dtype=np.complex128)
+        self.lib.ora_put_th(self.h, _d(a.view(np.float64)))
+
+    def get_th(self):
+        a = self.field()
+        self.lib.ora_get_th(self.h, _d(a.view(np.float64)))
+        return a
 
     def close(self):
         if self.h:

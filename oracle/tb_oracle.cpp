@@ -72,6 +72,8 @@ struct ora_ctx {
     std::vector<C> wx1, wy1, wz1, dv1x, dv1y, dv1z, dv2x, dv2y, dv2z;
     std::vector<C> d2uydx2;              // (nx, kfour)
     std::vector<C> fx, fy, fz;           // common /force/
+    std::vector<C> th, th1, dv1t, dv2t;  // thermal form: temperature and its RK storage
+    std::vector<double> thb;             // common /blast/ (nx, ny)
     // Poisson statistics of the last poi_uy
     std::vector<int> pv; std::vector<double> pres;
 
@@ -827,6 +829,7 @@ void bzone_impl(ora_ctx* o) {  // loop_par.f:6-45
             for (int i = 1; i <= o->nx; i++) {
                 size_t q = o->id(i, j, k);
                 double bd = (k == 3) ? o->bdfc2[i - 1] : o->bdfc[i - 1];   // bdt = 2 for k = 3
+                if (o->cfg.my_form == 2) o->th[q] = o->th[q] * bd;         // loop_par.f:36-39
                 o->wx[q] = o->wx[q] * bd;
                 o->wy[q] = o->wy[q] * bd;
                 if ((o->cfg.my_form == 0 || o->cfg.my_form == 4) && k == 1) {
@@ -1112,6 +1115,75 @@ void drv_gv_impl(ora_ctx* o, C* dvx, C* dvy, C* dvz) {
     }
 }
 
+// nlterms_th (nlterms_par.f:216-300) and drv_gvth (main_par.f:1404-1484):
+// the disturbance's full nonlinear products and those with the 2D base flow
+// and base temperature, the momentum terms of drv_gv (without its d dvarg/dx
+// term, commented out there) and the temperature equation.
+void drv_gvth_impl(ora_ctx* o, C* dvx, C* dvy, C* dvz, C* dvt) {
+    const size_t N3 = o->N3(), NP = (size_t)o->nx * o->ny * o->P;
+    std::vector<double> ph[7];
+    const std::vector<C>* in[7] = {&o->ux, &o->uy, &o->uz, &o->wx, &o->wy, &o->wz, &o->th};
+    for (int f = 0; f < 7; f++) { ph[f].assign(NP, 0.0); f_to_p_impl(o, ph[f].data(), in[f]->data()); }
+    for (size_t q = 0; q < NP; q++) {
+        const double ux = ph[0][q], uy = ph[1][q], uz = ph[2][q], wx = ph[3][q], wy = ph[4][q], wz = ph[5][q], th = ph[6][q];
+        ph[0][q] = uy * wx - ux * wy;
+        ph[1][q] = ux * wz - uz * wx;
+        ph[2][q] = uz * wy - uy * wz;
+        ph[3][q] = ux * ux;
+        ph[4][q] = ux * th;
+        ph[5][q] = uy * th;
+        ph[6][q] = uz * th;
+    }
+    std::vector<C> a(N3), b(N3), c(N3), d(N3), uth(N3), vth(N3), wth(N3);
+    std::vector<C>* out[7] = {&a, &b, &c, &d, &uth, &vth, &wth};
+    for (int f = 0; f < 7; f++) p_to_f_impl(o, out[f]->data(), ph[f].data());
+    for (int k = 1; k <= o->K; k++)
+        for (int j = 1; j <= o->ny; j++)
+            for (int i = 1; i <= o->nx; i++) {
+                size_t q = o->id(i, j, k), p = o->id2(i, j);
+                double U = o->uxb[p], V = o->uyb[p], W = o->wzb[p], T = o->thb[p];
+                a[q] = V * o->wx[q] - U * o->wy[q] + a[q];
+                b[q] = U * o->wz[q] + o->ux[q] * W + b[q];
+                c[q] = -V * o->wz[q] - o->uy[q] * W + c[q];
+                d[q] = 2.0 * U * o->ux[q] + d[q];
+                uth[q] = U * o->th[q] + o->ux[q] * T + uth[q];
+                vth[q] = V * o->th[q] + o->uy[q] * T + vth[q];
+                wth[q] = o->uz[q] * T + wth[q];
+            }
+    std::vector<C> dadx(N3), dbdx(N3), dddx(N3), duthdx(N3), dady(N3), dcdy(N3), dvthdy(N3), txx(N3), tyy(N3);
+    std::vector<C> xx[3] = {std::vector<C>(N3), std::vector<C>(N3), std::vector<C>(N3)};
+    std::vector<C> yy[3] = {std::vector<C>(N3), std::vector<C>(N3), std::vector<C>(N3)};
+    derparx_impl(o, dadx.data(), a.data());
+    derparx_impl(o, dbdx.data(), b.data());
+    derparx_impl(o, dddx.data(), d.data());
+    derparx_impl(o, duthdx.data(), uth.data());
+    dery_impl(o, dady.data(), a.data(), 0);
+    dery_impl(o, dcdy.data(), c.data(), 0);
+    dery_impl(o, dvthdy.data(), vth.data(), 0);
+    derparxx_impl(o, xx[0].data(), o->wx.data());
+    derparxx_impl(o, xx[1].data(), o->wy.data());
+    derparxx_impl(o, xx[2].data(), o->wz.data());
+    derparxx_impl(o, txx.data(), o->th.data());
+    dery_impl(o, yy[0].data(), o->wx.data(), 2);
+    dery_impl(o, yy[1].data(), o->wy.data(), 2);
+    dery_impl(o, yy[2].data(), o->wz.data(), 2);
+    dery_impl(o, tyy.data(), o->th.data(), 2);
+    const double Re = o->Re, fy = o->fac_y, varg = o->cfg.go_number * o->cfg.go_number / std::sqrt(Re);
+    const double RePr = Re * o->cfg.Pr;
+    for (int k = 1; k <= o->K; k++) {
+        C vkb = o->v_kb[k - 1];
+        double k2 = o->v_k2b2[k - 1];
+        for (int j = 2; j <= o->ny; j++)
+            for (int i = 1; i <= o->nx; i++) {
+                size_t q = o->id(i, j, k);
+                dvx[q] = -dady[q] + vkb * b[q] - vkb * d[q] * varg + (xx[0][q] + yy[0][q] * fy + k2 * o->wx[q]) / Re;
+                dvy[q] = -(vkb * c[q]) + dadx[q] + (xx[1][q] + yy[1][q] * fy + k2 * o->wy[q]) / Re;
+                dvz[q] = -dbdx[q] + dcdy[q] + varg * dddx[q] + (xx[2][q] + yy[2][q] * fy + k2 * o->wz[q]) / Re;
+                dvt[q] = -duthdx[q] - dvthdy[q] - vkb * wth[q] + (txx[q] + tyy[q] + k2 * o->th[q]) / RePr;
+            }
+    }
+}
+
 // les_par.f:6-211 (terms whose results the reference never uses -- the
 // x/y/z derivatives of nu_t and the nu_t spectrum -- are not formed).
 void les_terms_impl(ora_ctx* o, C* Fx, C* Fy, C* Fz) {
@@ -1205,6 +1277,7 @@ void cvirt_impl(ora_ctx* o, C* Fx, C* Fy, C* Fz) {  // immersed_par.f:262-313
 }
 void drv_impl(ora_ctx* o, C* dvx, C* dvy, C* dvz) {  // main_par.f:1264-1336 / 1487-1574
     if (o->cfg.my_form == 1) { drv_gv_impl(o, dvx, dvy, dvz); return; }
+    if (o->cfg.my_form == 2) { drv_gvth_impl(o, dvx, dvy, dvz, (dvx == o->dv1x.data() ? o->dv1t : o->dv2t).data()); return; }
     size_t N3 = o->N3();
     std::vector<C> a(N3), b(N3), c(N3), dadx(N3), dbdx(N3), dady(N3), dcdy(N3);
     std::vector<C> xx[3] = {std::vector<C>(N3), std::vector<C>(N3), std::vector<C>(N3)};
@@ -1461,7 +1534,8 @@ ora_ctx* ora_create(const tb_config* cfg) {
                     &o->dv2x, &o->dv2y, &o->dv2z, &o->fx, &o->fy, &o->fz})
         v->assign(N3, mk(0, 0));
     o->d2uydx2.assign((size_t)o->nx * o->K, mk(0, 0));
-    o->uxb.assign((size_t)o->nx * o->ny, 0.0); o->uyb = o->uxb; o->wzb = o->uxb;
+    o->uxb.assign((size_t)o->nx * o->ny, 0.0); o->uyb = o->uxb; o->wzb = o->uxb; o->thb = o->uxb;
+    for (auto* v : {&o->th, &o->th1, &o->dv1t, &o->dv2t}) v->assign(N3, mk(0, 0));
     o->duexmdx.assign(o->nx, 0.0);
     o->sp_poi.assign(7 * o->msh, 0); o->cp_poi.assign(8 * o->msh, 0); o->pp_poi.assign(4 * o->msh, 0); o->lp_poi.assign(5 * o->msh, 0);
     setup_constants(o);
@@ -1499,7 +1573,8 @@ int ora_init_fields(ora_ctx* o) {  // main_par.f:601-641
                     &o->dv2x, &o->dv2y, &o->dv2z, &o->fx, &o->fy, &o->fz})
         std::fill(v->begin(), v->end(), mk(0, 0));
     std::fill(o->d2uydx2.begin(), o->d2uydx2.end(), mk(0, 0));
-    if (o->cfg.my_form == 1) return 0;   // init_gv: every mode a disturbance, all zero
+    for (auto* v : {&o->th, &o->th1, &o->dv1t, &o->dv2t}) std::fill(v->begin(), v->end(), mk(0, 0));
+    if (o->cfg.my_form == 1 || o->cfg.my_form == 2) return 0;   // init_gv / init_gvth: every mode a disturbance, all zero
     for (int j = 1; j <= o->ny; j++)
         for (int i = 1; i <= o->nx; i++) {
             o->ux[o->id(i, j, 1)] = mk(o->uxb[o->id2(i, j)], 0.0);
@@ -1520,6 +1595,9 @@ int ora_get_state(ora_ctx* o, double* ux, double* uy, double* uz, double* wx, do
     return 0;
 }
 int ora_put_wall(ora_ctx* o, const double* d) { cp_in(o->d2uydx2, d); return 0; }
+int ora_set_baseflow_th(ora_ctx* o, const double* thb) { std::memcpy(o->thb.data(), thb, o->thb.size() * sizeof(double)); return 0; }
+int ora_put_th(ora_ctx* o, const double* th) { cp_in(o->th, th); return 0; }
+int ora_get_th(ora_ctx* o, double* th) { cp_out(th, o->th); return 0; }
 int ora_get_wall(ora_ctx* o, double* d) { cp_out(d, o->d2uydx2); return 0; }
 
 #define AS_C(p) reinterpret_cast<C*>(p)
@@ -1584,6 +1662,16 @@ int ora_rk_stage(ora_ctx* o, int stage, int t) {
                     o->wx[q] = o->wx1[q] + o->dt6 * (d1x[q] + d2x[q]);
                     o->wy[q] = o->wy1[q] + o->dt6 * (d1y[q] + d2y[q]);
                     o->wz[q] = o->wz1[q] + o->dt6 * (d1z[q] + d2z[q]);
+                }
+                if (c.my_form == 2) {   // main_par.f:366-440
+                    if (stage == 1) { o->th1[q] = o->th[q]; o->th[q] = o->th1[q] + o->dv1t[q] * o->dt2; }
+                    else if (stage == 2 || stage == 3) {
+                        double h = (stage == 2) ? o->dt2 : o->dt;
+                        o->th[q] = o->th1[q] + o->dv2t[q] * h;
+                        o->dv1t[q] = o->dv1t[q] + 2.0 * o->dv2t[q];
+                    } else {
+                        o->th[q] = o->th1[q] + o->dt6 * (o->dv1t[q] + o->dv2t[q]);
+                    }
                 }
             }
     if (stage == 1 || stage == 3) {

@@ -40,6 +40,9 @@ int      ora_get_state(ora_ctx* o, double* ux, double* uy, double* uz,
                        double* wx, double* wy, double* wz);
 int      ora_put_wall(ora_ctx* o, const double* d2uydx2);
 int      ora_get_wall(ora_ctx* o, double* d2uydx2);
+int      ora_set_baseflow_th(ora_ctx* o, const double* thb);   /* my_form 2: base temperature (nx, ny) */
+int      ora_put_th(ora_ctx* o, const double* th);             /* temperature disturbance (nx, ny, kfour) */
+int      ora_get_th(ora_ctx* o, double* th);
 
 int ora_derparx (ora_ctx* o, double* ddx,   const double* fc);
 int ora_derparxx(ora_ctx* o, double* d2dx2, const double* fc);

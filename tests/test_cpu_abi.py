@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol(lib_built):
 def test_bad_configs_are_rejected(lib_built):
     from trans_bl_gb300 import api
     bad = [dict(nx=66), dict(ny=30), dict(kphys=12), dict(kfour=9, kphys=16), dict(msh=1), dict(i2=5),
-           dict(precision=7), dict(my_form=2)]
+           dict(precision=7), dict(my_form=3), dict(my_form=2, ibm=1), dict(my_form=2, Pr=0.0)]
     for b in bad:
         cfg = api.default_config(**b)
         h = C.c_void_p()

@@ -131,3 +131,40 @@ def test_gortler_form_is_linear(lib_built, oracle_built):
         assert np.all(uy[0] == 0) and np.max(np.abs(uy[1:, 0, :])) > 0
     assert np.array_equal(out[0.0][1], out[8.0][1])
     assert not np.array_equal(out[0.0][0], out[8.0][0]) and not np.array_equal(out[0.0][2], out[8.0][2])
+
+
+def test_thermal_form_passive_and_linear(lib_built, oracle_built):
+    """drv_gvth: the temperature does not act on the momentum terms; without
+    a velocity disturbance and forcing the velocities stay zero and one step
+    of th is linear in th (doubling th doubles it); th keeps its zero wall
+    and top rows."""
+    from trans_bl_gb300 import configs
+    cfg = configs.thermal(make_default=oracle_built.default_config)
+    coefs, base = oracle_built.setup_inputs(cfg)
+    thb = configs.base_temperature(cfg, base)
+    rng = np.random.default_rng(57)
+    s = configs.disturbance_state(cfg, rng)
+    th = configs.smooth_random((cfg.kfour, cfg.ny, cfg.nx), rng, 1e-3)
+    th[:, 0, :] = 0.0
+    th[:, -1, :] = 0.0
+    o = oracle_built.Oracle(cfg, coefs, base)
+    o.set_baseflow_th(thb)
+    o.put_state(s)
+    o.put_th(np.zeros_like(th))
+    d0 = o.drv()
+    o.put_th(th)
+    d1 = o.drv()
+    for a, b in zip(d0, d1):
+        assert np.array_equal(a, b)
+    cfg.n_forced = 0
+    outs = []
+    for scale in (1.0, 2.0):
+        o = oracle_built.Oracle(cfg, coefs, base)
+        o.set_baseflow_th(thb)
+        o.put_th(scale * th)
+        o.step(cfg.stpp + 1)
+        outs.append(o.get_th())
+        assert all(np.max(np.abs(f)) == 0 for f in o.get_state().values())
+    assert rel(outs[1], 2.0 * outs[0]) < 1e-12
+    assert np.all(outs[0][:, 0, :] == 0) and np.all(outs[0][:, -1, :] == 0)
+    assert np.max(np.abs(outs[0] - th)) > 0

@@ -29,7 +29,7 @@ class TbConfig(C.Structure):
             "Re", "dx", "dy", "stf", "x0", "alpha", "omega", "beta", "fac_y", "alphaf", "tol_stage",
             "tol_final", "C_s", "A_plus", "irf", "ibm_xc", "ibm_zc", "ibm_h", "ibm_R")] + \
         [("n_forced", C.c_int), ("forced_mode", C.c_int * 4), ("forced_amp", C.c_double * 4),
-         ("forced_phase", C.c_double * 4), ("go_number", C.c_double)]
+         ("forced_phase", C.c_double * 4), ("go_number", C.c_double), ("Pr", C.c_double)]
 
     def as_dict(self):
         d = {}
@@ -98,6 +98,8 @@ def load():
     lib.tb_put_state.argtypes = [P] + [D] * 6
     lib.tb_get_state.argtypes = [P] + [D] * 6
     lib.tb_put_wall.argtypes = [P, D]
+    for n in ("tb_set_baseflow_th", "tb_put_th", "tb_get_th"):
+        getattr(lib, n).argtypes = [P, D]
     lib.tb_get_wall.argtypes = [P, D]
     lib.tb_rk_stage.argtypes = [P, C.c_int, C.c_int]
     lib.tb_step.argtypes = [P, C.c_int]
@@ -295,6 +297,20 @@ class Context:
         out = {n: self.field() for n in ("ux", "uy", "uz", "wx", "wy", "wz")}
         self._c(self.lib.tb_get_state(self.h, *[dptr(out[n].view(np.float64)) for n in
                                                 ("ux", "uy", "uz", "wx", "wy", "wz")]), "tb_get_state")
+        return out
+
+    def set_baseflow_th(self, thb):
+        """Base temperature thb(ny, nx) of the thermal form (tb_set_baseflow_th)."""
+        a = np.ascontiguousarray(thb, dtype=np.float64)
+        self._c(self.lib.tb_set_baseflow_th(self.h, dptr(a)), "tb_set_baseflow_th")
+
+    def put_th(self, th):
+        a = np.ascontiguousarray(th, dtype=np.complex128)
+        self._c(self.lib.tb_put_th(self.h, dptr(a.view(np.float64))), "tb_put_th")
+
+    def get_th(self):
+        out = self.field()
+        self._c(self.lib.tb_get_th(self.h, dptr(out.view(np.float64))), "tb_get_th")
         return out
 
     def put_wall(self, d2uydx2):

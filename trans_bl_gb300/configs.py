@@ -177,6 +177,23 @@ def gortler(nx=65, ny=33, kfour=4, kphys=8, msh=3, go_number=0.0, **kw):
     return cfg
 
 
+def thermal(nx=65, ny=33, kfour=4, kphys=8, msh=3, **kw):
+    """Thermal form (my_form 2, drv_gvth, main_par.f:1404-1484): the
+    disturbance with its full nonlinear products about the 2D base flow and
+    a transported temperature th (Prandtl number Pr, 0.72), forced by the TS
+    strip of ts2d_pert."""
+    return small(nx=nx, ny=ny, kfour=kfour, kphys=kphys, msh=msh, my_form=2, **kw)
+
+
+def base_temperature(cfg, base):
+    """A base temperature for the thermal form: thb = 1 - uxb / U_e, the
+    profile of a heated wall by Reynolds' analogy.  The reference reads its
+    thb from the 2D thermal base-flow marcher's output, which it does not
+    ship."""
+    uxb = base[0]
+    return 1.0 - uxb / uxb[-1:, :]
+
+
 NAMES = ("ux", "uy", "uz", "wx", "wy", "wz")
 
 

@@ -35,8 +35,12 @@ int check_cfg(const tb_config* c) {
     if (c->max_vcycles < 1) { tb_set_error("max_vcycles must be >= 1"); return TB_ERR_ARG; }
     if (c->n_forced < 0 || c->n_forced > 4) { tb_set_error("n_forced must be in [0, 4]"); return TB_ERR_ARG; }
     if (c->precision != TB_FORM_PLAIN_FP64 && c->precision != TB_FORM_MIXED) { tb_set_error("unknown precision form"); return TB_ERR_ARG; }
-    if (c->my_form != 0 && c->my_form != 1 && c->my_form != 4) { tb_set_error("my_form must be 0, 1 or 4"); return TB_ERR_ARG; }
-    if (c->my_form == 1 && c->ibm) { tb_set_error("my_form 1 (drv_gv) has no immersed-boundary term"); return TB_ERR_ARG; }
+    if (c->my_form < 0 || c->my_form > 4 || c->my_form == 3) { tb_set_error("my_form must be 0, 1, 2 or 4"); return TB_ERR_ARG; }
+    if ((c->my_form == 1 || c->my_form == 2) && c->ibm) {
+        tb_set_error("my_form %d (drv_gv/drv_gvth) has no immersed-boundary term", c->my_form);
+        return TB_ERR_ARG;
+    }
+    if (c->my_form == 2 && !(c->Pr > 0.0)) { tb_set_error("my_form 2 needs Pr > 0"); return TB_ERR_ARG; }
     if (c->les_damping < 0 || c->les_damping > 3) { tb_set_error("les_damping must be 0..3"); return TB_ERR_ARG; }
     return TB_OK;
 }
@@ -126,6 +130,14 @@ int tb_create(const tb_config* cfg, tb_ctx** out) {
         if ((r = dalloc(f, n3))) { tb_destroy(c); return r == TB_ERR_CUDA ? TB_ERR_NOMEM : r; }
     for (int q = 0; q < 24; q++)
         if ((r = dalloc(&c->tmp[q], n3))) { tb_destroy(c); return TB_ERR_NOMEM; }
+    if (cfg->my_form == 2) {   // the temperature, its RK storage, thb and nlterms_th's planes
+        if ((r = dalloc(&c->th, n3)) || (r = dalloc(&c->th1, n3)) || (r = dalloc(&c->dv1t, n3)) ||
+            (r = dalloc(&c->dv2t, n3)) || (r = dalloc(&c->thb, tb_n2(c))) ||
+            (r = dalloc(&c->th_phys, (size_t)7 * g.P * tb_n2(c)))) {
+            tb_destroy(c);
+            return TB_ERR_NOMEM;
+        }
+    }
     if ((r = dalloc(&c->d2uydx2, (size_t)g.nx * g.K)) || (r = dalloc(&c->lapv, (size_t)g.nx * g.K))) { tb_destroy(c); return TB_ERR_NOMEM; }
     size_t n2 = tb_n2(c);
     c->h_uxb.assign(n2, 0.0); c->h_uyb.assign(n2, 0.0); c->h_wzb.assign(n2, 0.0);
@@ -139,7 +151,7 @@ int tb_destroy(tb_ctx* c) {
     tb_mixed_free(c);
     void* ptrs[] = {c->ux, c->uy, c->uz, c->wx, c->wy, c->wz, c->wx1, c->wy1, c->wz1, c->dv1x, c->dv1y, c->dv1z, c->dv2x,
                     c->dv2y, c->dv2z, c->d2uydx2, c->lapv, c->uxb, c->uyb, c->wzb, c->duexmdx, c->bdfc, c->fcx, c->fcllx,
-                    c->fcx2, c->fcllx2, c->gibbs, c->delta_no, c->k2b2, c->tx1.a, c->tx1.g, c->tx1.ib, c->tx2.a, c->tx2.g, c->tx2.ib,
+                    c->fcx2, c->fcllx2, c->th, c->th1, c->dv1t, c->dv2t, c->thb, c->th_phys, c->gibbs, c->delta_no, c->k2b2, c->tx1.a, c->tx1.g, c->tx1.ib, c->tx2.a, c->tx2.g, c->tx2.ib,
                     c->tfil.a, c->tfil.g, c->tfil.ib,
                     c->tx1.hf, c->tx1.hb, c->tx1.pf, c->tx1.pb, c->tx2.hf, c->tx2.hb, c->tx2.pf, c->tx2.pb,
                     c->tfil.hf, c->tfil.hb, c->tfil.pf, c->tfil.pb,
@@ -207,9 +219,12 @@ int tb_init_fields(tb_ctx* c) {  // main_par.f:601-641
     for (cplx* f : fields) TB_CUDA(cudaMemsetAsync(f, 0, n3 * sizeof(cplx), c->stream));
     TB_CUDA(cudaMemsetAsync(c->d2uydx2, 0, (size_t)c->g.nx * c->g.K * sizeof(cplx), c->stream));
     size_t n2 = tb_n2(c);
-    // forms 0 and 4 carry the base flow in mode 0; the Goertler form's modes
-    // are all disturbances about it (init_gv zeroes every field)
-    if (c->cfg.my_form != 1) {
+    // forms 0 and 4 carry the base flow in mode 0; in the Goertler and
+    // thermal forms every mode is a disturbance about it (init_gv and
+    // init_gvth zero every field, the temperature too)
+    if (c->cfg.my_form == 2)
+        for (cplx* f : {c->th, c->th1, c->dv1t, c->dv2t}) TB_CUDA(cudaMemsetAsync(f, 0, n3 * sizeof(cplx), c->stream));
+    if (c->cfg.my_form != 1 && c->cfg.my_form != 2) {
         k_init_mode0<<<tb_blocks(n2, 256), 256, 0, c->stream>>>(c->ux, c->uy, c->wz, c->uxb, c->uyb, c->wzb, n2);
         TB_CHECK_LAUNCH(c);
     }
@@ -277,6 +292,25 @@ int tb_get_state(tb_ctx* c, double* ux, double* uy, double* uz, double* wx, doub
         (r = down_async(c, wx, c->wx, n3)) || (r = down_async(c, wy, c->wy, n3)) || (r = down_async(c, wz, c->wz, n3)))
         return r;
     return finish(c);
+}
+int tb_set_baseflow_th(tb_ctx* c, const double* thb) {
+    if (!c || !thb) { tb_set_error("null argument"); return TB_ERR_ARG; }
+    if (!c->thb) { tb_set_error("the base temperature exists in my_form 2 only"); return TB_ERR_STATE; }
+    TB_CUDA(cudaMemcpyAsync(c->thb, thb, tb_n2(c) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    tb_graph_reset(c);
+    return finish(c);
+}
+int tb_put_th(tb_ctx* c, const double* th) {
+    if (!c || !th) { tb_set_error("null argument"); return TB_ERR_ARG; }
+    if (!c->th) { tb_set_error("the temperature exists in my_form 2 only"); return TB_ERR_STATE; }
+    int r = up(c, c->th, th, tb_n3(c));
+    return r ? r : finish(c);
+}
+int tb_get_th(tb_ctx* c, double* th) {
+    if (!c || !th) { tb_set_error("null argument"); return TB_ERR_ARG; }
+    if (!c->th) { tb_set_error("the temperature exists in my_form 2 only"); return TB_ERR_STATE; }
+    int r = down_async(c, th, c->th, tb_n3(c));
+    return r ? r : finish(c);
 }
 int tb_put_wall(tb_ctx* c, const double* d) {
     if (!c || !d) { tb_set_error("null argument"); return TB_ERR_ARG; }

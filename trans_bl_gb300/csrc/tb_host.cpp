@@ -44,6 +44,7 @@ extern "C" int tb_config_default(tb_config* c) {
     c->C_s = 0.032; c->A_plus = 25.0; c->irf = -0.1 * c->Re;
     c->ibm_xc = 1.7; c->ibm_zc = 0.0; c->ibm_h = 0.0; c->ibm_R = 1e-2 / 0.1;
     c->n_forced = 1; c->forced_mode[0] = 0; c->forced_amp[0] = 1e-5; c->forced_phase[0] = 0.0;
+    c->Pr = 0.72;
     return TB_OK;
 }
 

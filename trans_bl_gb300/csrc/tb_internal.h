@@ -97,6 +97,11 @@ struct tb_ctx {
     double* uxb = nullptr; double* uyb = nullptr; double* wzb = nullptr; double* duexmdx = nullptr;
     double* bdfc = nullptr; double* fcx = nullptr; double* fcllx = nullptr; double* gibbs = nullptr;
     double* fcx2 = nullptr; double* fcllx2 = nullptr;   // Goertler strip (var_gv)
+    // thermal form (my_form 2): temperature disturbance, its RK storage, the
+    // base temperature, and the seven physical-space planes of nlterms_th
+    cplx *th = nullptr, *th1 = nullptr, *dv1t = nullptr, *dv2t = nullptr;
+    double* thb = nullptr;
+    double* th_phys = nullptr;
     double* delta_no = nullptr;  // (nx, ny, P) IBM indicator
     double* k2b2 = nullptr;      // (K)
     // line-operator tables
@@ -195,6 +200,13 @@ int tb_launch_cvirt(tb_ctx* c, cplx* fx, cplx* fy, cplx* fz, bool accumulate);
 int tb_delta_setup(tb_ctx* c);
 
 int tb_drv_k(tb_ctx* c, cplx* dvx, cplx* dvy, cplx* dvz);
+int tb_drv_gvth(tb_ctx* c, cplx* dvx, cplx* dvy, cplx* dvz, cplx* dvt);   // thermal form (tb_thermal.cu)
+int tb_combine_gv(tb_ctx* c, const cplx* dadx, const cplx* dady, const cplx* b, const cplx* xx0, const cplx* yy0,
+                  const cplx* cc, const cplx* xx1, const cplx* yy1, const cplx* dbdx, const cplx* dcdy,
+                  const cplx* xx2, const cplx* yy2, const cplx* d, const cplx* dddx, double varg, cplx* dvx, cplx* dvy,
+                  cplx* dvz);
+int tb_rk_update_th(tb_ctx* c, int stage);
+int tb_bzone_th(tb_ctx* c);
 int tb_drv_forced(tb_ctx* c, cplx* dvx, cplx* dvy, cplx* dvz, cplx* f[3], cplx* df[4]);
 int tb_rk_update(tb_ctx* c, int stage);
 int tb_loop_impl(tb_ctx* c, double erro, bool filter);

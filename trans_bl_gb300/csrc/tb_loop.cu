@@ -456,13 +456,21 @@ int tb_drv_gv(tb_ctx* c, cplx* dvx, cplx* dvy, cplx* dvz) {
                   {c->wx, t[10], YOP_D2}, {c->wy, t[11], YOP_D2}, {c->wz, t[12], YOP_D2}};
     if ((r = tb_launch_xlines(c, xj, 6))) return r;
     if ((r = tb_launch_ylines(c, yj, 5))) return r;
+    return tb_combine_gv(c, t[3], t[8], t[1], t[5], t[10], t[2], t[6], t[11], t[4], t[9], t[7], t[12], t[13], t[14],
+                         c->cfg.go_number * c->cfg.go_number / std::sqrt(c->cfg.Re), dvx, dvy, dvz);
+}
+
+// The momentum part of drv_gv / drv_gvth from its derivative fields.
+int tb_combine_gv(tb_ctx* c, const cplx* dadx, const cplx* dady, const cplx* b, const cplx* xx0, const cplx* yy0,
+                  const cplx* cc, const cplx* xx1, const cplx* yy1, const cplx* dbdx, const cplx* dcdy,
+                  const cplx* xx2, const cplx* yy2, const cplx* d, const cplx* dddx, double varg, cplx* dvx, cplx* dvy,
+                  cplx* dvz) {
     CombArgs A;
     std::memset(&A, 0, sizeof A);
-    A.dady = t[8]; A.b = t[1]; A.xx0 = t[5]; A.yy0 = t[10]; A.wx = c->wx;
-    A.c = t[2]; A.dadx = t[3]; A.xx1 = t[6]; A.yy1 = t[11]; A.wy = c->wy;
-    A.dbdx = t[4]; A.dcdy = t[9]; A.xx2 = t[7]; A.yy2 = t[12]; A.wz = c->wz;
-    A.gd = t[13]; A.gdddx = t[14];
-    A.varg = c->cfg.go_number * c->cfg.go_number / std::sqrt(c->cfg.Re);
+    A.dady = dady; A.b = b; A.xx0 = xx0; A.yy0 = yy0; A.wx = c->wx;
+    A.c = cc; A.dadx = dadx; A.xx1 = xx1; A.yy1 = yy1; A.wy = c->wy;
+    A.dbdx = dbdx; A.dcdy = dcdy; A.xx2 = xx2; A.yy2 = yy2; A.wz = c->wz;
+    A.gd = d; A.gdddx = dddx; A.varg = varg;
     A.dvx = dvx; A.dvy = dvy; A.dvz = dvz; A.k2b2 = c->k2b2;
     A.nx = c->g.nx; A.ny = c->g.ny; A.K = c->g.K; A.beta = c->cfg.beta; A.invRe = 1.0 / c->cfg.Re; A.fac_y = c->cfg.fac_y;
     k_combine<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(A);
@@ -475,6 +483,7 @@ int tb_drv_k(tb_ctx* c, cplx* dvx, cplx* dvy, cplx* dvz) {
     cplx** t = c->tmp;
     int r;
     if (c->cfg.my_form == 1) return tb_drv_gv(c, dvx, dvy, dvz);
+    if (c->cfg.my_form == 2) return tb_drv_gvth(c, dvx, dvy, dvz, dvx == c->dv1x ? c->dv1t : c->dv2t);
     if (c->cfg.my_form == 4 || c->cfg.ibm) {
         cplx* f[3] = {t[16], t[17], t[18]};
         cplx* df[4] = {t[19], t[20], t[21], t[22]};
@@ -537,7 +546,7 @@ int tb_rk_update(tb_ctx* c, int stage) {
              c->g.nx, c->g.ny, c->g.K, stage, c->dt, c->dt2, c->dt6};
     k_rk<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(A);
     TB_CHECK_LAUNCH(c);
-    return TB_OK;
+    return c->cfg.my_form == 2 ? tb_rk_update_th(c, stage) : TB_OK;
 }
 
 int tb_filter(tb_ctx* c) {
@@ -556,7 +565,7 @@ int tb_bzone_k(tb_ctx* c) {
     k_bzone<<<tb_blocks(tb_n3(c), 256), 256, 0, c->stream>>>(c->wx, c->wy, c->wz, c->bdfc, c->wzb, c->g.nx, c->g.ny, c->g.K, 0,
                                                               c->cfg.my_form);
     TB_CHECK_LAUNCH(c);
-    return TB_OK;
+    return c->cfg.my_form == 2 ? tb_bzone_th(c) : TB_OK;
 }
 int tb_bzonew_k(tb_ctx* c) {
     k_bzone<<<tb_blocks((size_t)c->g.nx * c->g.K, 256), 256, 0, c->stream>>>(c->wx, c->wy, c->wz, c->bdfc, c->wzb, c->g.nx,
