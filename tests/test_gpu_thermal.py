@@ -97,3 +97,32 @@ def test_temperature_only_in_the_thermal_form():
     with pytest.raises(api.TbError):
         g.put_th(np.zeros((cfg.kfour, cfg.ny, cfg.nx), dtype=np.complex128))
     g.close()
+
+
+def test_thermal_checkpoint(tmp_path):
+    """escreve's form-2 record (escreve_par.f:11-17): the step, then ux uy
+    uz wx wy wz th in one record; a fresh context reads the same state."""
+    import struct
+    from trans_bl_gb300 import api, configs
+    cfg = configs.thermal()
+    coefs, base = configs.setup_inputs(cfg)
+    rng = np.random.default_rng(74)
+    st = configs.disturbance_state(cfg, rng)
+    th = configs.smooth_random((cfg.kfour, cfg.ny, cfg.nx), rng, 1e-3)
+    g = api.Context(cfg, coefs, base)
+    g.put_state(st)
+    g.put_th(th)
+    path = str(tmp_path / "data_00.bin")
+    g.write_checkpoint(path, 17)
+    data = open(path, "rb").read()
+    n3 = cfg.nx * cfg.ny * cfg.kfour
+    assert struct.unpack("<i", data[:4])[0] == 4
+    assert struct.unpack("<i", data[12:16])[0] == 7 * n3 * 16
+    h = api.Context(cfg, coefs, base)
+    assert h.read_checkpoint(path) == 17
+    a = h.get_state()
+    for n in NAMES:
+        assert np.array_equal(a[n], st[n]), n
+    assert np.array_equal(h.get_th(), th)
+    g.close()
+    h.close()

@@ -101,17 +101,20 @@ int tb_io_set_subrecord_limit(long long bytes) {
     return TB_OK;
 }
 
+// escreve (escreve_par.f:6-30): record 1 the step, record 2 ux uy uz wx wy
+// wz, and th after them in the thermal form.
 int tb_write_checkpoint(tb_ctx* c, const char* path, int t) {
     if (!c || !path) { tb_set_error("null argument"); return TB_ERR_ARG; }
-    std::vector<cplx> h[6];
-    cplx* dev[6] = {c->ux, c->uy, c->uz, c->wx, c->wy, c->wz};
+    const int nf = c->cfg.my_form == 2 ? 7 : 6;
+    std::vector<cplx> h[7];
+    cplx* dev[7] = {c->ux, c->uy, c->uz, c->wx, c->wy, c->wz, c->th};
     int r;
-    for (int q = 0; q < 6; q++)
+    for (int q = 0; q < nf; q++)
         if ((r = download(c, dev[q], h[q]))) return r;
     FILE* f = std::fopen(path, "wb");
     if (!f) { tb_set_error("cannot open %s for writing", path); return TB_ERR_ARG; }
     std::vector<Piece> rec2;
-    for (auto& v : h) rec2.push_back({v.data(), v.size() * sizeof(cplx)});
+    for (int q = 0; q < nf; q++) rec2.push_back({h[q].data(), h[q].size() * sizeof(cplx)});
     int t32 = t;
     r = write_record(f, {{&t32, 4}});
     if (!r) r = write_record(f, rec2);
@@ -125,14 +128,15 @@ int tb_read_checkpoint(tb_ctx* c, const char* path, int* t) {
     FILE* f = std::fopen(path, "rb");
     if (!f) { tb_set_error("cannot open %s", path); return TB_ERR_ARG; }
     size_t n3 = tb_n3(c);
-    std::vector<cplx> all(6 * n3);
+    const int nf = c->cfg.my_form == 2 ? 7 : 6;
+    std::vector<cplx> all(nf * n3);
     int t32 = 0;
     int r = read_record(f, &t32, 4, path);
     if (!r) r = read_record(f, all.data(), all.size() * sizeof(cplx), path);
     std::fclose(f);
     if (r) return r;
-    cplx* dev[6] = {c->ux, c->uy, c->uz, c->wx, c->wy, c->wz};
-    for (int q = 0; q < 6; q++)
+    cplx* dev[7] = {c->ux, c->uy, c->uz, c->wx, c->wy, c->wz, c->th};
+    for (int q = 0; q < nf; q++)
         TB_CUDA(cudaMemcpyAsync(dev[q], all.data() + q * n3, n3 * sizeof(cplx), cudaMemcpyHostToDevice, c->stream));
     TB_CUDA(cudaStreamSynchronize(c->stream));
     tb_mixed_invalidate(c);
